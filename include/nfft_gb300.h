@@ -1,0 +1,218 @@
+/*
+ * nfft_gb300.h -- C ABI of the GB300 (sm_103a) NFFT plan.
+ *
+ * This is the boundary a host binding (Julia ccall, Python ctypes) calls.  It
+ * replaces the GPU plan of NFFT.jl's GPUArrays extension
+ * (ext/NFFTGPUArraysExt/implementation.jl) behind the AbstractNFFTs plan
+ * interface (AbstractNFFTs/src/interface.jl:170-243).  Each entry point names
+ * the reference interface it stands in for.
+ *
+ * Conventions (identical to NFFT.jl's):
+ *  - nodes k: D x M, column-major (coordinate index fastest), each coordinate
+ *    in [-1/2, 1/2];
+ *  - images f and oversampled grids g: column-major (dimension 1 fastest);
+ *  - complex values interleaved (re, im) of the plan's real type;
+ *  - forward:  fHat[j] = sum_n f[n] exp(-2 pi i k_j . (n - N/2)),
+ *    adjoint:  f[n]    = sum_j fHat[j] exp(+2 pi i k_j . (n - N/2)),
+ *    computed as B F D and D^H F^H B^H (docs/src/background.md:64-85).
+ *
+ * Data pointers passed to the transform calls are DEVICE pointers, except
+ * where a call says otherwise.  All transform calls are asynchronous on the
+ * plan's stream.  A plan is not safe for concurrent calls (it owns its
+ * oversampled grid, like NFFTPlan.tmpVec); independent plans are.
+ */
+#ifndef NFFT_GB300_H
+#define NFFT_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct nfft_plan nfft_plan;
+
+/* Status codes.  The Julia binding maps them onto the reference's exceptions:
+ * INVALID_ARG and NODE_OUT_OF_RANGE -> ArgumentError (src/utils.jl:46-55,
+ * src/convolution.jl:47-53), DIM_MISMATCH -> DimensionMismatch
+ * (src/utils.jl:98-105), UNSUPPORTED -> error() (src/windowFunctions.jl:16,
+ * src/precomputation.jl:401). */
+typedef enum {
+  NFFT_OK = 0,
+  NFFT_ERR_INVALID_ARG = 1,
+  NFFT_ERR_DIM_MISMATCH = 2,
+  NFFT_ERR_NODE_OUT_OF_RANGE = 3,
+  NFFT_ERR_ALLOC = 4,
+  NFFT_ERR_CUDA = 5,
+  NFFT_ERR_CUFFT = 6,
+  NFFT_ERR_TIMEOUT = 7,
+  NFFT_ERR_UNSUPPORTED = 8,
+  NFFT_ERR_NO_NODES = 9
+} nfft_status;
+
+/* Window functions, src/windowFunctions.jl:4-19. */
+enum {
+  NFFT_WINDOW_KAISER_BESSEL = 0,
+  NFFT_WINDOW_GAUSS = 1,
+  NFFT_WINDOW_SPLINE = 2,
+  NFFT_WINDOW_KAISER_BESSEL_REV = 3,
+  NFFT_WINDOW_COSH_TYPE = 4
+};
+
+/* PrecomputeFlags, AbstractNFFTs/src/misc.jl:13-19.  On the device FULL
+ * evaluates the window function itself per tap (no stored sparse matrix),
+ * TENSOR and POLYNOMIAL evaluate the fitted polynomial of
+ * src/precomputation.jl:302-320 per tap, LINEAR interpolates the
+ * LUT of src/precomputation.jl:291-300. */
+enum {
+  NFFT_PRECOMPUTE_FULL = 1,
+  NFFT_PRECOMPUTE_TENSOR = 2,
+  NFFT_PRECOMPUTE_LINEAR = 3,
+  NFFT_PRECOMPUTE_POLYNOMIAL = 4
+};
+
+enum { NFFT_F32 = 32, NFFT_F64 = 64 };
+
+/* NFFTParams (src/implementation.jl:3-14).  m and sigma are final values:
+ * the host binding applies accuracyParams (AbstractNFFTs/src/misc.jl:66-81)
+ * before calling. */
+typedef struct {
+  int32_t m;                /* window half width (taps per dimension: 2m), 2..8 */
+  double sigma;             /* oversampling factor; Ntilde = 2*ceil(sigma*N/2) */
+  int32_t window;           /* NFFT_WINDOW_* */
+  int32_t precompute;       /* NFFT_PRECOMPUTE_* */
+  int32_t blocking;         /* 1: bin-sorted tiled kernels; 0: per-node kernels
+                               with global atomics (the plain path) */
+  int32_t sort_nodes;       /* accepted for interface parity; nodes are always
+                               binned on the device when blocking = 1 */
+  int32_t store_deconv_idx; /* accepted for interface parity; deconvolution is
+                               fused with padding/cropping */
+  int64_t block_size[3];    /* tile (block) size per dimension; 0 = automatic */
+  int32_t compensated;      /* 1: compensated (Kahan) spreading tiles */
+  int32_t timing;           /* 1: record per-stage device times (TimingStats) */
+} nfft_params;
+
+/* Plan geometry as NFFTPlan exposes it (N, NOut, J, Ntilde, params). */
+typedef struct {
+  int32_t precision;        /* 32 or 64 */
+  int32_t D;
+  int64_t N[3];
+  int64_t Ntilde[3];
+  int64_t M;                /* J, number of nodes */
+  int32_t m;
+  double sigma;
+  int32_t window;
+  int32_t precompute;
+  int64_t lut_size;         /* LUTSize, src/precomputation.jl:14-17 */
+  int64_t block_size[3];
+  int64_t num_tiles;
+  int64_t num_spread_tasks; /* after nfft_set_nodes */
+  int64_t num_spread_entries;
+  int64_t scratch_bytes;    /* device bytes held by the plan */
+} nfft_info;
+
+/* Fill defaults of NFFTParams for the GPU plan (m = 4, sigma = 2,
+ * kaiser_bessel, POLYNOMIAL, blocking). */
+void nfft_params_default(nfft_params* params);
+
+/* plan_nfft(CuArray, k, N; kwargs...) without the nodes:
+ * AbstractNFFTs.plan_nfft(::NFFTBackend, ::Type{<:AbstractGPUArray}, ...)
+ * (ext/NFFTGPUArraysExt/implementation.jl:21-59).  Builds Ntilde
+ * (src/precomputation.jl:3-56), the cuFFT plans, the deconvolution factors
+ * (src/precomputation.jl:347-358, on the device in FP64) and the window
+ * tables.  stream may be NULL (legacy default stream). */
+int nfft_plan_create(nfft_plan** plan, int precision, int D, const int64_t* N, int64_t M,
+                     const nfft_params* params, void* stream);
+
+/* Finalizer; frees every device buffer the plan holds. */
+int nfft_plan_destroy(nfft_plan* plan);
+
+/* copy(p): an independent plan with the same nodes
+ * (src/implementation.jl:45-66). */
+int nfft_plan_copy(const nfft_plan* plan, nfft_plan** out);
+
+/* Rebind the plan to another stream (CUDA.jl's task-local stream). */
+int nfft_set_stream(nfft_plan* plan, void* stream);
+
+/* nodes!(p, k) (AbstractNFFTs/src/interface.jl:208-213,
+ * src/implementation.jl:108-141): checks the nodes like checkNodes
+ * (src/utils.jl:46-55), reduces them to grid index and fractional offset,
+ * bins them with a stable device radix sort (src/precomputation.jl:487-520)
+ * and builds the spreading task list.  k is D x M of the plan's real type;
+ * k_on_device selects a device or a host pointer.  Synchronises the stream. */
+int nfft_set_nodes(nfft_plan* plan, const void* k, int k_on_device);
+
+/* mul!(fHat, p, f) (src/implementation.jl:155-172,
+ * ext/NFFTGPUArraysExt/implementation.jl:97-115): fused pad + apodize,
+ * forward FFT, gather interpolation. */
+int nfft_forward(nfft_plan* plan, const void* f, void* fhat);
+
+/* mul!(f, adjoint(p), fHat) (src/implementation.jl:176-193,
+ * ext/NFFTGPUArraysExt/implementation.jl:118-136): spreading, backward
+ * (unnormalised) FFT, fused crop + apodize. */
+int nfft_adjoint(nfft_plan* plan, const void* fhat, void* f);
+
+/* convolve!(p, g, fHat) (AbstractNFFTs/src/interface.jl:221-232,
+ * src/convolution.jl:20-53).  g has size Ntilde.  A flag of 1 marks a real
+ * array (the sampling-density client, NFFTTools/src/samplingDensity.jl:105-112);
+ * complex g with real fHat is rejected (ArgumentError). */
+int nfft_convolve(nfft_plan* plan, const void* g, int g_real, void* fhat, int fhat_real);
+
+/* convolve_transpose!(p, fHat, g) (AbstractNFFTs/src/interface.jl:235-243,
+ * src/convolution.jl:115-149).  Complex fHat with real g is rejected. */
+int nfft_convolve_transpose(nfft_plan* plan, const void* fhat, int fhat_real, void* g, int g_real);
+
+/* deconvolve!(p, f, g) (src/deconvolution.jl:2-45): writes the whole
+ * oversampled grid g (zeros outside the image). */
+int nfft_deconvolve(nfft_plan* plan, const void* f, void* g);
+
+/* deconvolve_transpose!(p, g, f) (src/deconvolution.jl:49-92). */
+int nfft_deconvolve_transpose(nfft_plan* plan, const void* g, void* f);
+
+/* Node gradient (no reference counterpart: the reference rrules return
+ * NoTangent for k, AbstractNFFTs/ext/AbstractNFFTsChainRulesCoreExt.jl:45,61).
+ * dk[d, j] = Re( conj(w[j]) * d(A(k) v)_j / dk[d, j] ), with A the forward
+ * NFFT; v has size N, w has length M, dk is D x M of the real type.  For a
+ * loss of y = A f use (v, w) = (f, ybar); for a loss of x = A^H y use
+ * (v, w) = (xbar, y). */
+int nfft_grad_nodes(nfft_plan* plan, const void* v, const void* w, void* dk);
+
+/* Plan geometry and sizes. */
+int nfft_get_info(const nfft_plan* plan, nfft_info* info);
+
+/* Device pointer of the plan's oversampled grid (NFFTPlan.tmpVec). */
+void* nfft_grid(nfft_plan* plan);
+
+/* TimingStats (AbstractNFFTs/src/misc.jl:22-30): device seconds of the last
+ * transforms as {pre, conv, fft, deconv, conv_adjoint, fft_adjoint,
+ * deconv_adjoint}.  Synchronises the stream. */
+int nfft_get_timing(nfft_plan* plan, double out[7]);
+
+/* Integer outputs of the binning, copied to host buffers (the reference's
+ * nodesInBlock, src/precomputation.jl:487-520): perm[i] = node at sorted
+ * position i (0-based), tile_start (num_tiles+1) = CSR offsets of the tiles,
+ * grid_index (D x M) = first grid index of each node's window per
+ * dimension, (trunc(k*Ntilde) - m + 1) mod Ntilde.  Any pointer may be NULL. */
+int nfft_get_binning(nfft_plan* plan, int32_t* perm, int32_t* tile_start, int32_t* grid_index);
+
+/* Deconvolution factors 1/phi-hat per dimension (windowHatInvLUT,
+ * src/precomputation.jl:347-358), copied to a host buffer of N[0]+..+N[D-1]
+ * values of the plan's real type. */
+int nfft_get_deconv_factors(nfft_plan* plan, void* out);
+
+/* Wait for the plan's stream. */
+int nfft_sync(nfft_plan* plan);
+
+/* Number of kernels this library has launched in the calling process. */
+int64_t nfft_kernel_launch_count(void);
+
+const char* nfft_status_string(int status);
+
+/* Message of the last failing call on this host thread. */
+const char* nfft_last_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* NFFT_GB300_H */

@@ -1,0 +1,321 @@
+// Internal declarations of the GB300 NFFT plan: plan object, device helpers,
+// window evaluation and kernel launchers.  Only the C ABI in
+// include/nfft_gb300.h is public.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cufft.h>
+#include <stdint.h>
+#include <atomic>
+#include <string>
+
+#include "../../include/nfft_gb300.h"
+
+namespace nfft {
+
+constexpr int kMaxDim = 3;
+constexpr int kMinM = 2;
+constexpr int kMaxM = 8;
+constexpr int kMaxL = 2 * kMaxM;
+constexpr int kMaxDeg = 2 * kMaxM + 1;
+constexpr int kChebNodes = 30;  // ChebyshevInterpolator(κ, 1, N, 30), src/precomputation.jl:351
+
+// Window evaluation modes on the device.
+enum WinMode { WIN_POLY = 0, WIN_LINEAR = 1, WIN_EXACT = 2 };
+
+extern std::atomic<int64_t> g_launches;
+void set_error(const char* fmt, ...);
+
+#define NFFT_CUDA_TRY(expr)                                                              \
+  do {                                                                                   \
+    cudaError_t err__ = (expr);                                                          \
+    if (err__ != cudaSuccess) {                                                          \
+      ::nfft::set_error("%s:%d: %s: %s", __FILE__, __LINE__, #expr,                     \
+                        cudaGetErrorString(err__));                                      \
+      return NFFT_ERR_CUDA;                                                              \
+    }                                                                                    \
+  } while (0)
+
+#define NFFT_LAUNCH_CHECK()                                                              \
+  do {                                                                                   \
+    ::nfft::g_launches.fetch_add(1, std::memory_order_relaxed);                          \
+    cudaError_t err__ = cudaGetLastError();                                              \
+    if (err__ != cudaSuccess) {                                                          \
+      ::nfft::set_error("%s:%d: kernel launch: %s", __FILE__, __LINE__,                 \
+                        cudaGetErrorString(err__));                                      \
+      return NFFT_ERR_CUDA;                                                              \
+    }                                                                                    \
+  } while (0)
+
+// Per-launch geometry shared by the convolution kernels (passed by value).
+template <typename T> struct Geom {
+  int D;
+  int m;
+  int Nt[kMaxDim];        // oversampled grid, singleton dims = 1
+  int bs[kMaxDim];        // tile size, singleton dims = 1
+  int ntiles[kMaxDim];
+  int64_t plane;          // Nt[0]*Nt[1]
+  int64_t M;
+  int mode;               // WinMode
+  int window;             // NFFT_WINDOW_*
+  T sigma;
+  T lut_scale;            // LUTSize / m (LINEAR)
+  const T* coeffs;        // (2m+1) x 2m, column l contiguous (POLY)
+  const T* lut;           // LUTSize+2 (LINEAR)
+  bool small_grid;        // some Ntilde < 2m: taps may wrap more than once
+};
+
+// Sorted node data produced by nfft_set_nodes.
+template <typename T> struct Nodes {
+  const int32_t* perm;    // sorted position -> node id
+  const int32_t* ti;      // D x M (SoA, dim-major): trunc(k_shift * Ntilde), sorted order
+  const T* te;            // D x M (SoA): fractional offset e in [0,1) (slightly outside for FP32)
+  int64_t M;
+};
+
+}  // namespace nfft
+
+struct nfft_plan {
+  int precision = 32;
+  int D = 0;
+  int64_t N[3] = {1, 1, 1};
+  int64_t Nt[3] = {1, 1, 1};
+  int64_t M = 0;
+  nfft_params prm{};
+  int m = 4;
+  double sigma = 2.0;
+  int64_t lut_size = 0;
+  int64_t bs[3] = {1, 1, 1};
+  int64_t ntiles[3] = {1, 1, 1};
+  int64_t ntiles_total = 1;
+  cudaStream_t stream = nullptr;
+  cufftHandle fft = 0;
+  bool fft_ok = false;
+  size_t real_size = 4;
+
+  void* grid = nullptr;       // tmpVec, |Ntilde| complex
+  void* inv = nullptr;        // deconvolution factors, N0+N1+N2 reals
+  void* coeffs = nullptr;     // poly coefficients (T)
+  void* lut = nullptr;        // LINEAR lut (T)
+  double coeffs_host[nfft::kMaxDeg * nfft::kMaxL] = {};
+
+  bool has_nodes = false;
+  void* k = nullptr;          // D x M nodes (T), user order
+  int32_t* perm = nullptr;    // M
+  int32_t* ti = nullptr;      // D x M sorted
+  void* te = nullptr;         // D x M sorted (T)
+  int32_t* tile_start = nullptr;   // ntiles_total + 1 (nodes per home tile)
+  void* cbuf = nullptr;       // M complex scratch for real-valued convolve calls (lazy)
+  // spreading task list (owner-computes tiles)
+  int64_t n_entries = 0;
+  int32_t* entries = nullptr;      // sorted node ids grouped by tile
+  int64_t n_tasks = 0;
+  int4* tasks = nullptr;           // (tile, begin, end, multi)
+  int64_t n_multi = 0;
+  int32_t* multi_tiles = nullptr;  // tiles written by more than one task
+  int* dflag = nullptr;            // device status word
+  size_t scratch_bytes = 0;
+
+  bool timing_on = false;
+  cudaEvent_t ev[4] = {};
+  double timing[7] = {};
+};
+
+namespace nfft {
+
+// ------------------------------------------------------------------ launchers
+// precompute.cu
+int launch_check_nodes(const nfft_plan* p, const void* k, int* flag);
+int launch_reduce_nodes(const nfft_plan* p, const void* k, int32_t* ti_u, void* te_u, uint32_t* key,
+                        int32_t* val, int32_t* tile_count);
+int launch_gather_sorted(const nfft_plan* p, const int32_t* perm, const int32_t* ti_u, const void* te_u);
+int launch_deconv_factors(nfft_plan* p);
+int launch_count_entries(const nfft_plan* p, int32_t* ecount);
+int launch_fill_entries(const nfft_plan* p, const int32_t* eoff, uint32_t* ekey, int32_t* eval,
+                        int32_t* tcount);
+int launch_build_tasks(nfft_plan* p, const int32_t* tile_estart, int chunk);
+// sort.cu
+int radix_sort_pairs(uint32_t* keys, int32_t* vals, uint32_t* keys_tmp, int32_t* vals_tmp, int64_t n,
+                     int key_bits, void* scratch, size_t scratch_bytes, cudaStream_t s,
+                     uint32_t** keys_out, int32_t** vals_out);
+size_t radix_sort_scratch_bytes(int64_t n);
+int exclusive_scan_i32(const int32_t* in, int32_t* out, int64_t n, void* scratch, size_t scratch_bytes,
+                       cudaStream_t s);
+size_t scan_scratch_bytes(int64_t n);
+// deconv.cu
+int launch_pad_apodize(const nfft_plan* p, const void* f, void* g);
+int launch_crop_apodize(const nfft_plan* p, const void* g, void* f);
+int launch_real_to_complex(const nfft_plan* p, const void* in, void* out, int64_t n);
+int launch_real_part(const nfft_plan* p, const void* in, void* out, int64_t n);
+// interp.cu
+int launch_interp(const nfft_plan* p, const void* g, int g_real, void* fhat, int fhat_real);
+// spread.cu
+int launch_spread(nfft_plan* p, const void* fhat, int fhat_real, void* g, int g_real);
+// gradk.cu
+int launch_grad_nodes(const nfft_plan* p, const void* g, const void* w, void* dk);
+// plain.cu (per-node kernels of the plain path, blocking = 0)
+int launch_plain_interp(const nfft_plan* p, const void* g, int g_real, void* fhat, int fhat_real);
+int launch_plain_spread(const nfft_plan* p, const void* fhat, int fhat_real, void* g, int g_real);
+
+template <typename T> Geom<T> make_geom(const nfft_plan* p);
+template <typename T> Nodes<T> make_nodes(const nfft_plan* p);
+
+// ------------------------------------------------------------ device helpers
+
+__host__ __device__ inline int wrap_once(int g, int n) { return g < 0 ? g + n : (g >= n ? g - n : g); }
+__host__ __device__ inline int wrap_any(int g, int n) {
+  int r = g % n;
+  return r < 0 ? r + n : r;
+}
+
+template <typename T> struct Cplx;
+template <> struct Cplx<float> { using type = float2; };
+template <> struct Cplx<double> { using type = double2; };
+
+template <typename T> __device__ inline T dev_sqrt(T x);
+template <> __device__ inline float dev_sqrt<float>(float x) { return sqrtf(x); }
+template <> __device__ inline double dev_sqrt<double>(double x) { return sqrt(x); }
+
+// Modified Bessel I0 from its power series sum_k (x^2/4)^k / (k!)^2.
+template <typename T> __host__ __device__ inline T bessel_i0_series(T x) {
+  T q = T(0.25) * x * x, term = T(1), sum = T(1);
+  for (int k = 1; k < 200; ++k) {
+    term *= q / (T(k) * T(k));
+    sum += term;
+    if (term <= sum * T(1e-17)) break;
+  }
+  return sum;
+}
+
+// Bessel J0 from its power series sum_k (-x^2/4)^k / (k!)^2 (moderate x only).
+template <typename T> __host__ __device__ inline T bessel_j0_series(T x) {
+  T q = -T(0.25) * x * x, term = T(1), sum = T(1);
+  for (int k = 1; k < 200; ++k) {
+    term *= q / (T(k) * T(k));
+    sum += term;
+    if (term <= sum * T(1e-18) && term >= -sum * T(1e-18) && k > 4) break;
+  }
+  return sum;
+}
+
+// Cardinal B-spline of order n at x (src/windowFunctions.jl:75-87),
+// evaluated bottom-up over the shifts it needs.
+template <typename T> __host__ __device__ inline T cbspline_eval(int n, T x) {
+  T b[2 * kMaxM + 2];
+  for (int j = 0; j < n; ++j) b[j] = (x - T(j) >= T(0) && x - T(j) < T(1)) ? T(1) : T(0);
+  for (int o = 2; o <= n; ++o) {
+    for (int j = 0; j + o <= n; ++j) {
+      T xs = x - T(j);
+      b[j] = xs / T(o - 1) * b[j] + (T(o) - xs) / T(o - 1) * b[j + 1];
+    }
+  }
+  return b[0];
+}
+
+// Window phi at distance x (grid units), i.e. phi(x/Ntilde) of
+// src/windowFunctions.jl with the Ntilde factors cancelled.
+template <typename T> __host__ __device__ inline T window_exact(int window, T x, int m, T sigma) {
+  const T PI = T(3.14159265358979323846);
+  T ax = x < T(0) ? -x : x;
+  T mm = T(m);
+  switch (window) {
+    case NFFT_WINDOW_KAISER_BESSEL: {
+      T b = PI * (T(2) - T(1) / sigma);
+      if (ax < mm) {
+        T arg = sqrt(mm * mm - x * x);
+        return sinh(b * arg) / (arg * PI);
+      } else if (ax > mm) {
+        return T(0);
+      }
+      return b / PI;
+    }
+    case NFFT_WINDOW_GAUSS: {
+      T b = mm / PI;
+      if (ax < mm) return T(1) / sqrt(PI * b) * exp(-(x * x) / b);
+      return T(0);
+    }
+    case NFFT_WINDOW_SPLINE:
+      if (ax < mm) return cbspline_eval<T>(2 * m, x + mm);
+      return T(0);
+    case NFFT_WINDOW_KAISER_BESSEL_REV: {
+      T b = PI * (T(2) - T(1) / sigma);
+      if (ax < mm) {
+        T r = x / mm;
+        return T(0.5) / mm * bessel_i0_series<T>(mm * b * sqrt(T(1) - r * r));
+      }
+      return T(0);
+    }
+    case NFFT_WINDOW_COSH_TYPE: {
+      T beta = PI * mm * (T(2) - T(1) / sigma);
+      if (ax < mm) {
+        T a = x / mm;
+        T alpha = sqrt(T(1) - a * a);
+        return T(1) / (cosh(beta) - T(1)) * (cosh(beta * alpha) - T(1)) / alpha;
+      }
+      return T(0);
+    }
+  }
+  return T(0);
+}
+
+__device__ __forceinline__ float add_rn(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ double add_rn(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ float mul_rn(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ double mul_rn(double a, double b) { return __dmul_rn(a, b); }
+
+// Reduce node j, dimension d.  The grid index follows NFFT.jl's blocked path
+// exactly in the plan's real type T: shiftNodes! (src/utils.jl:32-44), then
+// unsafe_trunc(Int, k*Ntilde) (src/precomputation.jl:496,536), so that bin
+// ids and grid indices are bit-identical.  The fractional offset is formed in
+// FP64: for T = Float64 it is the reference's own kscale - trunc; for
+// T = Float32 it is the exact k*Ntilde (+Ntilde for shifted nodes) minus the
+// index, which avoids the Float32 rounding of k + 1.
+template <typename T>
+__device__ __forceinline__ void reduce_coord(T x, int Nt, int32_t& t_out, T& e_out) {
+  T xs = x;
+  if (xs < T(0)) xs = add_rn(xs, T(1));
+  if (xs == T(1)) xs = xs - (sizeof(T) == 4 ? T(1.1920928955078125e-7) : T(2.220446049250313080847e-16));
+  T ks = mul_rn(xs, T(Nt));
+  int t = int(ks);
+  if (t >= Nt) t = Nt - 1;
+  if (t < 0) t = 0;
+  double e;
+  if (sizeof(T) == 4) {
+    e = double(x) * double(Nt) + (x < T(0) ? double(Nt) : 0.0) - double(t);
+  } else {
+    e = double(ks) - double(t);
+  }
+  t_out = t;
+  e_out = T(e);
+}
+
+// Window value of tap l (0-based) for a node with fractional offset e:
+// the tap sits at trunc - m + 1 + l, the node at trunc + e.
+template <typename T>
+__device__ __forceinline__ T tap_weight(const Geom<T>& G, const T* __restrict__ coeffs_smem, T e, int l) {
+  if (G.mode == WIN_POLY) {
+    // evalpoly(e - 1/2, coeffs[:, l]), src/precomputation.jl:205-222
+    const int deg = 2 * G.m + 1;
+    const T* c = coeffs_smem + l * deg;
+    T t = e - T(0.5);
+    T r = c[deg - 1];
+    for (int i = deg - 2; i >= 0; --i) r = fma(r, t, c[i]);
+    return r;
+  } else if (G.mode == WIN_LINEAR) {
+    // linear LUT interpolation of phi(|x|), src/precomputation.jl:168-190
+    T x = e + T(G.m - 1 - l);
+    T u = (x < T(0) ? -x : x) * G.lut_scale;
+    // the LUT holds LUTSize+2 samples; an offset a hair outside [0,1)
+    // (FP32 nodes) must not index past them
+    const T umax = T(G.m) * G.lut_scale;
+    if (u > umax) u = umax;
+    T fi = floor(u);
+    int i = int(fi);
+    T a = u - fi;
+    T v0 = __ldg(G.lut + i), v1 = __ldg(G.lut + i + 1);
+    return v0 + a * (v1 - v0);
+  }
+  return window_exact<T>(G.window, e + T(G.m - 1 - l), G.m, G.sigma);
+}
+
+}  // namespace nfft

@@ -1,0 +1,762 @@
+// C ABI of the GB300 NFFT plan (include/nfft_gb300.h): plan construction,
+// node binning, forward/adjoint orchestration, cuFFT, timing, errors.
+#include "nfft_internal.cuh"
+
+#include <chrono>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <vector>
+
+namespace nfft {
+
+std::atomic<int64_t> g_launches{0};
+static thread_local char g_err[1024] = "";
+
+void set_error(const char* fmt, ...) {
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(g_err, sizeof(g_err), fmt, ap);
+  va_end(ap);
+}
+
+template <typename T> Geom<T> make_geom(const nfft_plan* p) {
+  Geom<T> G{};
+  G.D = p->D;
+  G.m = p->m;
+  bool small = false;
+  for (int d = 0; d < kMaxDim; ++d) {
+    G.Nt[d] = int(p->Nt[d]);
+    G.bs[d] = int(p->bs[d]);
+    G.ntiles[d] = int(p->ntiles[d]);
+    if (d < p->D && p->Nt[d] < 2 * p->m) small = true;
+  }
+  G.plane = p->Nt[0] * p->Nt[1];
+  G.M = p->M;
+  G.mode = (p->prm.precompute == NFFT_PRECOMPUTE_FULL)     ? WIN_EXACT
+           : (p->prm.precompute == NFFT_PRECOMPUTE_LINEAR) ? WIN_LINEAR
+                                                           : WIN_POLY;
+  G.window = p->prm.window;
+  G.sigma = T(p->sigma);
+  G.lut_scale = T(p->lut_size / p->m);
+  G.coeffs = static_cast<const T*>(p->coeffs);
+  G.lut = static_cast<const T*>(p->lut);
+  G.small_grid = small;
+  return G;
+}
+template Geom<float> make_geom<float>(const nfft_plan*);
+template Geom<double> make_geom<double>(const nfft_plan*);
+
+template <typename T> Nodes<T> make_nodes(const nfft_plan* p) {
+  Nodes<T> n{};
+  n.perm = p->perm;
+  n.ti = p->ti;
+  n.te = static_cast<const T*>(p->te);
+  n.M = p->M;
+  return n;
+}
+template Nodes<float> make_nodes<float>(const nfft_plan*);
+template Nodes<double> make_nodes<double>(const nfft_plan*);
+
+namespace {
+
+// --------------------------------------------------------------- host math
+
+// Householder least squares min ||A x - b|| for a tall rows x cols matrix
+// (column-major), FP64.  Used for the window polynomial fit.
+bool lstsq(std::vector<double> A, std::vector<double> b, int rows, int cols, double* x) {
+  for (int c = 0; c < cols; ++c) {
+    double norm = 0;
+    for (int r = c; r < rows; ++r) norm += A[r + rows * c] * A[r + rows * c];
+    norm = std::sqrt(norm);
+    if (norm == 0) return false;
+    double alpha = A[c + rows * c] > 0 ? -norm : norm;
+    std::vector<double> v(rows, 0.0);
+    for (int r = c; r < rows; ++r) v[r] = A[r + rows * c];
+    v[c] -= alpha;
+    double vn = 0;
+    for (int r = c; r < rows; ++r) vn += v[r] * v[r];
+    if (vn == 0) continue;
+    for (int cc = c; cc < cols; ++cc) {
+      double s = 0;
+      for (int r = c; r < rows; ++r) s += v[r] * A[r + rows * cc];
+      s = 2 * s / vn;
+      for (int r = c; r < rows; ++r) A[r + rows * cc] -= s * v[r];
+    }
+    double s = 0;
+    for (int r = c; r < rows; ++r) s += v[r] * b[r];
+    s = 2 * s / vn;
+    for (int r = c; r < rows; ++r) b[r] -= s * v[r];
+  }
+  for (int c = cols - 1; c >= 0; --c) {
+    double s = b[c];
+    for (int cc = c + 1; cc < cols; ++cc) s -= A[c + rows * cc] * x[cc];
+    x[c] = s / A[c + rows * c];
+  }
+  return true;
+}
+
+// precomputePolyInterp, src/precomputation.jl:302-320: for tap column l a
+// least-squares fit (V' \ samples) of a degree-2m polynomial in t to
+// phi(m - (l - 0.5) + t), sampled at 2(2m+1) equispaced t in [-0.5, 0.5].
+bool poly_fit(int window, int m, double sigma, double* out /* deg x 2m, column l contiguous */) {
+  const int deg = 2 * m + 1, K = 2 * m, ns = 2 * deg;
+  std::vector<double> A(size_t(ns) * deg), t(ns);
+  for (int i = 0; i < ns; ++i) t[i] = -0.5 + double(i) / double(ns - 1);
+  for (int r = 0; r < deg; ++r)
+    for (int i = 0; i < ns; ++i) A[i + ns * r] = std::pow(t[i], double(r));
+  for (int l = 1; l <= K; ++l) {
+    std::vector<double> b(ns);
+    for (int i = 0; i < ns; ++i) b[i] = window_exact<double>(window, (m - (l - 0.5)) + t[i], m, sigma);
+    if (!lstsq(A, b, ns, deg, out + size_t(l - 1) * deg)) return false;
+  }
+  return true;
+}
+
+// LUT of src/precomputation.jl:291-300: phi(l * m / K), l = 0..K+1.
+template <typename T> __global__ void lut_kernel(int window, int m, double sigma, int64_t K, T* out) {
+  int64_t l = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (l >= K + 2) return;
+  out[l] = T(window_exact<double>(window, double(l) * double(m) / double(K), m, sigma));
+}
+
+int64_t lut_size_for(int m) {
+  static const int m2K[] = {1, 3, 7, 9, 14, 17, 20, 23, 24};
+  int K = m2K[(m + 1 < 9 ? m + 1 : 9) - 1];
+  return (int64_t(1) << K) * m;
+}
+
+void default_block(nfft_plan* p) {
+  // Tiles of about 4096 points in FP32 (32 KiB of accumulators), halved in
+  // FP64; the reference's blockSize keyword overrides them.
+  int64_t def[3][3] = {{4096, 1, 1}, {64, 64, 1}, {16, 16, 16}};
+  for (int d = 0; d < 3; ++d) {
+    int64_t b = def[p->D - 1][d];
+    if (p->precision == 64 && d == p->D - 1) b = b > 1 ? b / 2 : 1;
+    if (p->prm.block_size[d] > 0 && d < p->D) b = p->prm.block_size[d];
+    if (d >= p->D) b = 1;
+    if (b > p->Nt[d]) b = p->Nt[d];
+    p->bs[d] = b;
+  }
+}
+
+void free_nodes(nfft_plan* p) {
+  cudaFree(p->k);
+  cudaFree(p->perm);
+  cudaFree(p->ti);
+  cudaFree(p->te);
+  cudaFree(p->tile_start);
+  cudaFree(p->entries);
+  cudaFree(p->tasks);
+  cudaFree(p->multi_tiles);
+  p->k = p->te = nullptr;
+  p->perm = p->ti = p->tile_start = p->entries = p->multi_tiles = nullptr;
+  p->tasks = nullptr;
+  p->n_entries = p->n_tasks = p->n_multi = 0;
+  p->has_nodes = false;
+}
+
+int bits_for(int64_t n) {
+  int b = 0;
+  while ((int64_t(1) << b) < n) ++b;
+  return b;
+}
+
+struct DevBuf {
+  void* p = nullptr;
+  ~DevBuf() { cudaFree(p); }
+  bool alloc(size_t n) { return cudaMalloc(&p, n ? n : 16) == cudaSuccess; }
+};
+
+#define NFFT_ALLOC(buf, bytes)                                                         \
+  do {                                                                                 \
+    if (!(buf).alloc(bytes)) {                                                         \
+      set_error("cudaMalloc of %zu bytes failed", size_t(bytes));                      \
+      return NFFT_ERR_ALLOC;                                                           \
+    }                                                                                  \
+  } while (0)
+
+int cufft_check(cufftResult r, const char* what) {
+  if (r != CUFFT_SUCCESS) {
+    set_error("cuFFT %s failed (%d)", what, int(r));
+    return NFFT_ERR_CUFFT;
+  }
+  return NFFT_OK;
+}
+
+int exec_fft(nfft_plan* p, int dir) {
+  if (p->precision == 32) {
+    auto* g = static_cast<cufftComplex*>(p->grid);
+    return cufft_check(cufftExecC2C(p->fft, g, g, dir), "exec");
+  }
+  auto* g = static_cast<cufftDoubleComplex*>(p->grid);
+  return cufft_check(cufftExecZ2Z(p->fft, g, g, dir), "exec");
+}
+
+void record(nfft_plan* p, int i) {
+  if (p->timing_on) cudaEventRecord(p->ev[i], p->stream);
+}
+
+void collect_timing(nfft_plan* p, int base) {
+  if (!p->timing_on) return;
+  cudaEventSynchronize(p->ev[3]);
+  float a = 0, b = 0, c = 0;
+  cudaEventElapsedTime(&a, p->ev[0], p->ev[1]);
+  cudaEventElapsedTime(&b, p->ev[1], p->ev[2]);
+  cudaEventElapsedTime(&c, p->ev[2], p->ev[3]);
+  if (base == 0) {  // forward: deconv, fft, conv
+    p->timing[3] = a * 1e-3;
+    p->timing[2] = b * 1e-3;
+    p->timing[1] = c * 1e-3;
+  } else {  // adjoint: conv, fft, deconv
+    p->timing[4] = a * 1e-3;
+    p->timing[5] = b * 1e-3;
+    p->timing[6] = c * 1e-3;
+  }
+}
+
+}  // namespace
+}  // namespace nfft
+
+using namespace nfft;
+
+extern "C" {
+
+void nfft_params_default(nfft_params* prm) {
+  if (!prm) return;
+  std::memset(prm, 0, sizeof(*prm));
+  prm->m = 4;
+  prm->sigma = 2.0;
+  prm->window = NFFT_WINDOW_KAISER_BESSEL;
+  prm->precompute = NFFT_PRECOMPUTE_POLYNOMIAL;
+  prm->blocking = 1;
+}
+
+const char* nfft_status_string(int s) {
+  switch (s) {
+    case NFFT_OK: return "ok";
+    case NFFT_ERR_INVALID_ARG: return "invalid argument";
+    case NFFT_ERR_DIM_MISMATCH: return "dimension mismatch";
+    case NFFT_ERR_NODE_OUT_OF_RANGE: return "node out of range";
+    case NFFT_ERR_ALLOC: return "device allocation failed";
+    case NFFT_ERR_CUDA: return "CUDA error";
+    case NFFT_ERR_CUFFT: return "cuFFT error";
+    case NFFT_ERR_TIMEOUT: return "timeout";
+    case NFFT_ERR_UNSUPPORTED: return "unsupported";
+    case NFFT_ERR_NO_NODES: return "plan has no nodes";
+  }
+  return "unknown status";
+}
+
+const char* nfft_last_error(void) { return g_err; }
+
+int64_t nfft_kernel_launch_count(void) { return g_launches.load(); }
+
+int nfft_plan_create(nfft_plan** out, int precision, int D, const int64_t* N, int64_t M, const nfft_params* prm_in,
+                     void* stream) {
+  if (!out || !N) {
+    set_error("null argument");
+    return NFFT_ERR_INVALID_ARG;
+  }
+  *out = nullptr;
+  nfft_params prm;
+  if (prm_in) prm = *prm_in;
+  else nfft_params_default(&prm);
+  if (precision != 32 && precision != 64) {
+    set_error("precision must be 32 or 64");
+    return NFFT_ERR_INVALID_ARG;
+  }
+  if (D < 1 || D > 3) {
+    set_error("D = %d not supported (1..3)", D);
+    return NFFT_ERR_UNSUPPORTED;
+  }
+  if (M < 0 || M > (int64_t(1) << 30)) {
+    set_error("M = %lld out of range", (long long)M);
+    return NFFT_ERR_INVALID_ARG;
+  }
+  if (prm.m < kMinM || prm.m > kMaxM) {
+    set_error("m = %d not supported (2..8)", prm.m);
+    return NFFT_ERR_UNSUPPORTED;
+  }
+  if (!(prm.sigma >= 1.0) || prm.sigma > 16.0) {
+    set_error("sigma = %g out of range [1, 16]", prm.sigma);
+    return NFFT_ERR_INVALID_ARG;
+  }
+  if (prm.window < 0 || prm.window > 4) {
+    set_error("Window %d not yet implemented!", prm.window);
+    return NFFT_ERR_UNSUPPORTED;
+  }
+  if (prm.precompute < 1 || prm.precompute > 4) {
+    set_error("precompute = %d not supported by NFFT.jl!", prm.precompute);
+    return NFFT_ERR_UNSUPPORTED;
+  }
+  auto* p = new nfft_plan();
+  p->precision = precision;
+  p->real_size = precision == 32 ? 4 : 8;
+  p->D = D;
+  p->M = M;
+  p->prm = prm;
+  p->m = prm.m;
+  p->stream = static_cast<cudaStream_t>(stream);
+  int64_t total = 1;
+  for (int d = 0; d < D; ++d) {
+    if (N[d] < 1) {
+      delete p;
+      set_error("N[%d] = %lld must be positive", d, (long long)N[d]);
+      return NFFT_ERR_INVALID_ARG;
+    }
+    p->N[d] = N[d];
+    // Ntilde = (ceil(sigma*N) ÷ 2) * 2, src/precomputation.jl:25-27
+    p->Nt[d] = (int64_t(std::ceil(prm.sigma * double(N[d]))) / 2) * 2;
+    if (p->Nt[d] < 2) p->Nt[d] = 2;
+    if (p->Nt[d] >= (int64_t(1) << 30)) {
+      delete p;
+      set_error("oversampled size too large");
+      return NFFT_ERR_UNSUPPORTED;
+    }
+    total *= p->Nt[d];
+  }
+  if (total >= (int64_t(1) << 34)) {
+    delete p;
+    set_error("oversampled grid of %lld points too large", (long long)total);
+    return NFFT_ERR_UNSUPPORTED;
+  }
+  p->sigma = double(p->Nt[0]) / double(p->N[0]);  // sigma = Ntilde/N, :30
+  p->lut_size = lut_size_for(p->m);
+  default_block(p);
+  p->ntiles_total = 1;
+  for (int d = 0; d < 3; ++d) {
+    p->ntiles[d] = (p->Nt[d] + p->bs[d] - 1) / p->bs[d];
+    p->ntiles_total *= p->ntiles[d];
+  }
+  if (p->ntiles_total >= (int64_t(1) << 31)) {
+    delete p;
+    set_error("too many tiles");
+    return NFFT_ERR_UNSUPPORTED;
+  }
+  const size_t rs = p->real_size;
+  auto fail = [&](int rc) {
+    nfft_plan_destroy(p);
+    return rc;
+  };
+  if (cudaMalloc(&p->grid, 2 * rs * size_t(total)) != cudaSuccess) {
+    set_error("cudaMalloc of the oversampled grid (%zu bytes) failed", size_t(2 * rs * total));
+    return fail(NFFT_ERR_ALLOC);
+  }
+  p->scratch_bytes += 2 * rs * size_t(total);
+  const int64_t ninv = p->N[0] + (D > 1 ? p->N[1] : 0) + (D > 2 ? p->N[2] : 0) + 1;
+  const int deg = 2 * p->m + 1, L = 2 * p->m;
+  if (cudaMalloc(&p->inv, rs * ninv) != cudaSuccess || cudaMalloc(&p->coeffs, rs * deg * L) != cudaSuccess ||
+      cudaMalloc(&p->dflag, sizeof(int)) != cudaSuccess) {
+    set_error("cudaMalloc of plan tables failed");
+    return fail(NFFT_ERR_ALLOC);
+  }
+  // window polynomial (FP64 fit on the host, stored in T like Matrix{T})
+  if (!poly_fit(prm.window, p->m, p->sigma, p->coeffs_host)) {
+    set_error("window polynomial fit failed");
+    return fail(NFFT_ERR_INVALID_ARG);
+  }
+  {
+    std::vector<unsigned char> buf(rs * deg * L);
+    for (int q = 0; q < deg * L; ++q) {
+      if (precision == 32) reinterpret_cast<float*>(buf.data())[q] = float(p->coeffs_host[q]);
+      else reinterpret_cast<double*>(buf.data())[q] = p->coeffs_host[q];
+    }
+    if (cudaMemcpy(p->coeffs, buf.data(), buf.size(), cudaMemcpyHostToDevice) != cudaSuccess) {
+      set_error("upload of window coefficients failed");
+      return fail(NFFT_ERR_CUDA);
+    }
+    // trailing "one" factor used for singleton dimensions
+    unsigned char one[8];
+    if (precision == 32) { float v = 1.0f; std::memcpy(one, &v, 4); }
+    else { double v = 1.0; std::memcpy(one, &v, 8); }
+    if (cudaMemcpy(static_cast<char*>(p->inv) + rs * (ninv - 1), one, rs, cudaMemcpyHostToDevice) != cudaSuccess) {
+      set_error("upload failed");
+      return fail(NFFT_ERR_CUDA);
+    }
+  }
+  if (prm.precompute == NFFT_PRECOMPUTE_LINEAR) {
+    const int64_t K = p->lut_size;
+    if (cudaMalloc(&p->lut, rs * size_t(K + 2)) != cudaSuccess) {
+      set_error("cudaMalloc of the window LUT failed");
+      return fail(NFFT_ERR_ALLOC);
+    }
+    p->scratch_bytes += rs * size_t(K + 2);
+    const unsigned nb = unsigned((K + 2 + 255) / 256);
+    if (precision == 32) lut_kernel<float><<<nb, 256, 0, p->stream>>>(prm.window, p->m, p->sigma, K, static_cast<float*>(p->lut));
+    else lut_kernel<double><<<nb, 256, 0, p->stream>>>(prm.window, p->m, p->sigma, K, static_cast<double*>(p->lut));
+    g_launches.fetch_add(1);
+  }
+  int rc = launch_deconv_factors(p);
+  if (rc) return fail(rc);
+  // cuFFT: Julia's column-major Ntilde is C-order reversed
+  int n[3];
+  for (int d = 0; d < D; ++d) n[d] = int(p->Nt[D - 1 - d]);
+  rc = cufft_check(cufftPlanMany(&p->fft, D, n, nullptr, 1, 0, nullptr, 1, 0,
+                                 precision == 32 ? CUFFT_C2C : CUFFT_Z2Z, 1),
+                   "plan");
+  if (rc) return fail(rc);
+  p->fft_ok = true;
+  rc = cufft_check(cufftSetStream(p->fft, p->stream), "set stream");
+  if (rc) return fail(rc);
+  if (prm.timing) {
+    p->timing_on = true;
+    for (int i = 0; i < 4; ++i) cudaEventCreate(&p->ev[i]);
+  }
+  if (cudaStreamSynchronize(p->stream) != cudaSuccess || cudaGetLastError() != cudaSuccess) {
+    set_error("plan construction failed on the device");
+    return fail(NFFT_ERR_CUDA);
+  }
+  *out = p;
+  return NFFT_OK;
+}
+
+int nfft_plan_destroy(nfft_plan* p) {
+  if (!p) return NFFT_OK;
+  free_nodes(p);
+  cudaFree(p->grid);
+  cudaFree(p->inv);
+  cudaFree(p->coeffs);
+  cudaFree(p->lut);
+  cudaFree(p->dflag);
+  cudaFree(p->cbuf);
+  if (p->fft_ok) cufftDestroy(p->fft);
+  if (p->timing_on)
+    for (int i = 0; i < 4; ++i) cudaEventDestroy(p->ev[i]);
+  delete p;
+  return NFFT_OK;
+}
+
+int nfft_set_stream(nfft_plan* p, void* stream) {
+  if (!p) return NFFT_ERR_INVALID_ARG;
+  p->stream = static_cast<cudaStream_t>(stream);
+  return cufft_check(cufftSetStream(p->fft, p->stream), "set stream");
+}
+
+int nfft_set_nodes(nfft_plan* p, const void* k, int k_on_device) {
+  if (!p || (!k && p->M > 0)) {
+    set_error("null argument");
+    return NFFT_ERR_INVALID_ARG;
+  }
+  auto t0 = std::chrono::steady_clock::now();
+  free_nodes(p);
+  const int64_t M = p->M, D = p->D;
+  const size_t rs = p->real_size;
+  cudaStream_t s = p->stream;
+  if (cudaMalloc(&p->k, rs * size_t(D * M > 0 ? D * M : 1)) != cudaSuccess ||
+      cudaMalloc(&p->perm, sizeof(int32_t) * size_t(M > 0 ? M : 1)) != cudaSuccess ||
+      cudaMalloc(&p->ti, sizeof(int32_t) * size_t(D * M > 0 ? D * M : 1)) != cudaSuccess ||
+      cudaMalloc(&p->te, rs * size_t(D * M > 0 ? D * M : 1)) != cudaSuccess ||
+      cudaMalloc(&p->tile_start, sizeof(int32_t) * size_t(p->ntiles_total + 1)) != cudaSuccess) {
+    free_nodes(p);
+    set_error("cudaMalloc of node arrays failed");
+    return NFFT_ERR_ALLOC;
+  }
+  if (M > 0) {
+    NFFT_CUDA_TRY(cudaMemcpyAsync(p->k, k, rs * size_t(D * M),
+                                  k_on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, s));
+  }
+  // checkNodes
+  int flag = 0;
+  NFFT_CUDA_TRY(cudaMemsetAsync(p->dflag, 0, sizeof(int), s));
+  int rc = launch_check_nodes(p, p->k, p->dflag);
+  if (rc) return rc;
+  NFFT_CUDA_TRY(cudaMemcpyAsync(&flag, p->dflag, sizeof(int), cudaMemcpyDeviceToHost, s));
+  NFFT_CUDA_TRY(cudaStreamSynchronize(s));
+  if (flag) {
+    free_nodes(p);
+    set_error("Nodes k need to be within the range [-1/2, 1/2)");
+    return NFFT_ERR_NODE_OUT_OF_RANGE;
+  }
+  const int64_t nt = p->ntiles_total;
+  const int kbits = bits_for(nt);
+  {
+    // reduce + stable radix sort by home tile
+    DevBuf ti_u, te_u, key, val, key2, val2, tcount, scr;
+    NFFT_ALLOC(ti_u, sizeof(int32_t) * size_t(D * M));
+    NFFT_ALLOC(te_u, rs * size_t(D * M));
+    NFFT_ALLOC(key, sizeof(uint32_t) * size_t(M));
+    NFFT_ALLOC(val, sizeof(int32_t) * size_t(M));
+    NFFT_ALLOC(key2, sizeof(uint32_t) * size_t(M));
+    NFFT_ALLOC(val2, sizeof(int32_t) * size_t(M));
+    NFFT_ALLOC(tcount, sizeof(int32_t) * size_t(nt + 1));
+    const size_t sb = std::max(radix_sort_scratch_bytes(M), scan_scratch_bytes(nt + 1));
+    NFFT_ALLOC(scr, sb);
+    NFFT_CUDA_TRY(cudaMemsetAsync(tcount.p, 0, sizeof(int32_t) * size_t(nt + 1), s));
+    rc = launch_reduce_nodes(p, p->k, static_cast<int32_t*>(ti_u.p), te_u.p, static_cast<uint32_t*>(key.p),
+                             static_cast<int32_t*>(val.p), static_cast<int32_t*>(tcount.p));
+    if (rc) return rc;
+    uint32_t* ko = nullptr;
+    int32_t* vo = nullptr;
+    rc = radix_sort_pairs(static_cast<uint32_t*>(key.p), static_cast<int32_t*>(val.p), static_cast<uint32_t*>(key2.p),
+                          static_cast<int32_t*>(val2.p), M, kbits, scr.p, sb, s, &ko, &vo);
+    if (rc) return rc;
+    if (M > 0) NFFT_CUDA_TRY(cudaMemcpyAsync(p->perm, vo, sizeof(int32_t) * size_t(M), cudaMemcpyDeviceToDevice, s));
+    rc = exclusive_scan_i32(static_cast<int32_t*>(tcount.p), p->tile_start, nt + 1, scr.p, sb, s);
+    if (rc) return rc;
+    rc = launch_gather_sorted(p, p->perm, static_cast<int32_t*>(ti_u.p), te_u.p);
+    if (rc) return rc;
+    NFFT_CUDA_TRY(cudaStreamSynchronize(s));
+  }
+  p->scratch_bytes = size_t(2) * rs * size_t(p->Nt[0] * p->Nt[1] * p->Nt[2]) + rs * size_t(D * M) * 2 +
+                     sizeof(int32_t) * size_t(M + D * M + nt + 1);
+  if (p->prm.blocking) {
+    // spreading entries: (tile, sorted node) pairs for every tile a window touches
+    DevBuf ecount, eoff, scr;
+    NFFT_ALLOC(ecount, sizeof(int32_t) * size_t(M + 1));
+    NFFT_ALLOC(eoff, sizeof(int32_t) * size_t(M + 1));
+    const size_t sb1 = scan_scratch_bytes(std::max<int64_t>(M + 1, nt + 1));
+    NFFT_ALLOC(scr, sb1);
+    NFFT_CUDA_TRY(cudaMemsetAsync(ecount.p, 0, sizeof(int32_t) * size_t(M + 1), s));
+    rc = launch_count_entries(p, static_cast<int32_t*>(ecount.p));
+    if (rc) return rc;
+    rc = exclusive_scan_i32(static_cast<int32_t*>(ecount.p), static_cast<int32_t*>(eoff.p), M + 1, scr.p, sb1, s);
+    if (rc) return rc;
+    int32_t E = 0;
+    NFFT_CUDA_TRY(cudaMemcpyAsync(&E, static_cast<int32_t*>(eoff.p) + M, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+    NFFT_CUDA_TRY(cudaStreamSynchronize(s));
+    if (E < 0) {
+      set_error("too many spreading entries");
+      return NFFT_ERR_UNSUPPORTED;
+    }
+    DevBuf ekey, eval, ekey2, eval2, tcount, tstart, scr2;
+    NFFT_ALLOC(ekey, sizeof(uint32_t) * size_t(E));
+    NFFT_ALLOC(eval, sizeof(int32_t) * size_t(E));
+    NFFT_ALLOC(ekey2, sizeof(uint32_t) * size_t(E));
+    NFFT_ALLOC(eval2, sizeof(int32_t) * size_t(E));
+    NFFT_ALLOC(tcount, sizeof(int32_t) * size_t(nt + 1));
+    NFFT_ALLOC(tstart, sizeof(int32_t) * size_t(nt + 1));
+    const size_t sb2 = std::max(radix_sort_scratch_bytes(E), scan_scratch_bytes(nt + 1));
+    NFFT_ALLOC(scr2, sb2);
+    NFFT_CUDA_TRY(cudaMemsetAsync(tcount.p, 0, sizeof(int32_t) * size_t(nt + 1), s));
+    rc = launch_fill_entries(p, static_cast<int32_t*>(eoff.p), static_cast<uint32_t*>(ekey.p),
+                             static_cast<int32_t*>(eval.p), static_cast<int32_t*>(tcount.p));
+    if (rc) return rc;
+    uint32_t* ko = nullptr;
+    int32_t* vo = nullptr;
+    rc = radix_sort_pairs(static_cast<uint32_t*>(ekey.p), static_cast<int32_t*>(eval.p),
+                          static_cast<uint32_t*>(ekey2.p), static_cast<int32_t*>(eval2.p), E, kbits, scr2.p, sb2, s,
+                          &ko, &vo);
+    if (rc) return rc;
+    if (cudaMalloc(&p->entries, sizeof(int32_t) * size_t(E > 0 ? E : 1)) != cudaSuccess) {
+      set_error("cudaMalloc of spreading entries failed");
+      return NFFT_ERR_ALLOC;
+    }
+    if (E > 0) NFFT_CUDA_TRY(cudaMemcpyAsync(p->entries, vo, sizeof(int32_t) * size_t(E), cudaMemcpyDeviceToDevice, s));
+    p->n_entries = E;
+    rc = exclusive_scan_i32(static_cast<int32_t*>(tcount.p), static_cast<int32_t*>(tstart.p), nt + 1, scr2.p, sb2, s);
+    if (rc) return rc;
+    rc = launch_build_tasks(p, static_cast<int32_t*>(tstart.p), 2048);
+    if (rc) return rc;
+    p->scratch_bytes += sizeof(int32_t) * size_t(E);
+  }
+  NFFT_CUDA_TRY(cudaStreamSynchronize(s));
+  NFFT_CUDA_TRY(cudaGetLastError());
+  p->has_nodes = true;
+  p->timing[0] = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  return NFFT_OK;
+}
+
+int nfft_plan_copy(const nfft_plan* src, nfft_plan** out) {
+  if (!src || !out) return NFFT_ERR_INVALID_ARG;
+  int rc = nfft_plan_create(out, src->precision, src->D, src->N, src->M, &src->prm, src->stream);
+  if (rc) return rc;
+  if (src->has_nodes) {
+    rc = nfft_set_nodes(*out, src->k, 1);
+    if (rc) {
+      nfft_plan_destroy(*out);
+      *out = nullptr;
+    }
+  }
+  return rc;
+}
+
+static int require_nodes(const nfft_plan* p) {
+  if (!p) {
+    set_error("null plan");
+    return NFFT_ERR_INVALID_ARG;
+  }
+  if (!p->has_nodes) {
+    set_error("plan has no nodes: call nfft_set_nodes first");
+    return NFFT_ERR_NO_NODES;
+  }
+  return NFFT_OK;
+}
+
+int nfft_forward(nfft_plan* p, const void* f, void* fhat) {
+  int rc = require_nodes(p);
+  if (rc) return rc;
+  record(p, 0);
+  rc = launch_pad_apodize(p, f, p->grid);
+  if (rc) return rc;
+  record(p, 1);
+  rc = exec_fft(p, CUFFT_FORWARD);
+  if (rc) return rc;
+  record(p, 2);
+  rc = p->prm.blocking ? launch_interp(p, p->grid, 0, fhat, 0) : launch_plain_interp(p, p->grid, 0, fhat, 0);
+  if (rc) return rc;
+  record(p, 3);
+  if (p->timing_on) collect_timing(p, 0);
+  return NFFT_OK;
+}
+
+int nfft_adjoint(nfft_plan* p, const void* fhat, void* f) {
+  int rc = require_nodes(p);
+  if (rc) return rc;
+  record(p, 0);
+  rc = p->prm.blocking ? launch_spread(p, fhat, 0, p->grid, 0) : launch_plain_spread(p, fhat, 0, p->grid, 0);
+  if (rc) return rc;
+  record(p, 1);
+  rc = exec_fft(p, CUFFT_INVERSE);
+  if (rc) return rc;
+  record(p, 2);
+  rc = launch_crop_apodize(p, p->grid, f);
+  if (rc) return rc;
+  record(p, 3);
+  if (p->timing_on) collect_timing(p, 1);
+  return NFFT_OK;
+}
+
+static int ensure_cbuf(nfft_plan* p) {
+  if (p->cbuf) return NFFT_OK;
+  if (cudaMalloc(&p->cbuf, 2 * p->real_size * size_t(p->M > 0 ? p->M : 1)) != cudaSuccess) {
+    set_error("cudaMalloc of the node scratch failed");
+    return NFFT_ERR_ALLOC;
+  }
+  return NFFT_OK;
+}
+
+int nfft_convolve(nfft_plan* p, const void* g, int g_real, void* fhat, int fhat_real) {
+  int rc = require_nodes(p);
+  if (rc) return rc;
+  if (!g_real && fhat_real) {
+    set_error("Complex input g requires Complex output fHat");
+    return NFFT_ERR_INVALID_ARG;
+  }
+  const void* src = g;
+  void* dst = fhat;
+  if (g_real) {  // real grid -> the plan's complex grid
+    rc = launch_real_to_complex(p, g, p->grid, p->Nt[0] * p->Nt[1] * p->Nt[2]);
+    if (rc) return rc;
+    src = p->grid;
+  }
+  if (fhat_real) {
+    if ((rc = ensure_cbuf(p))) return rc;
+    dst = p->cbuf;
+  }
+  rc = p->prm.blocking ? launch_interp(p, src, 0, dst, 0) : launch_plain_interp(p, src, 0, dst, 0);
+  if (rc) return rc;
+  if (fhat_real) rc = launch_real_part(p, dst, fhat, p->M);
+  return rc;
+}
+
+int nfft_convolve_transpose(nfft_plan* p, const void* fhat, int fhat_real, void* g, int g_real) {
+  int rc = require_nodes(p);
+  if (rc) return rc;
+  if (!fhat_real && g_real) {
+    set_error("Complex input fHat requires Complex output g");
+    return NFFT_ERR_INVALID_ARG;
+  }
+  const void* src = fhat;
+  void* dst = g_real ? p->grid : g;
+  if (fhat_real) {
+    if ((rc = ensure_cbuf(p))) return rc;
+    rc = launch_real_to_complex(p, fhat, p->cbuf, p->M);
+    if (rc) return rc;
+    src = p->cbuf;
+  }
+  rc = p->prm.blocking ? launch_spread(p, src, 0, dst, 0) : launch_plain_spread(p, src, 0, dst, 0);
+  if (rc) return rc;
+  if (g_real) rc = launch_real_part(p, dst, g, p->Nt[0] * p->Nt[1] * p->Nt[2]);
+  return rc;
+}
+
+int nfft_deconvolve(nfft_plan* p, const void* f, void* g) {
+  if (!p) return NFFT_ERR_INVALID_ARG;
+  return launch_pad_apodize(p, f, g);
+}
+
+int nfft_deconvolve_transpose(nfft_plan* p, const void* g, void* f) {
+  if (!p) return NFFT_ERR_INVALID_ARG;
+  return launch_crop_apodize(p, g, f);
+}
+
+int nfft_grad_nodes(nfft_plan* p, const void* v, const void* w, void* dk) {
+  int rc = require_nodes(p);
+  if (rc) return rc;
+  rc = launch_pad_apodize(p, v, p->grid);
+  if (rc) return rc;
+  rc = exec_fft(p, CUFFT_FORWARD);
+  if (rc) return rc;
+  return launch_grad_nodes(p, p->grid, w, dk);
+}
+
+int nfft_get_info(const nfft_plan* p, nfft_info* info) {
+  if (!p || !info) return NFFT_ERR_INVALID_ARG;
+  std::memset(info, 0, sizeof(*info));
+  info->precision = p->precision;
+  info->D = p->D;
+  for (int d = 0; d < 3; ++d) {
+    info->N[d] = p->N[d];
+    info->Ntilde[d] = p->Nt[d];
+    info->block_size[d] = p->bs[d];
+  }
+  info->M = p->M;
+  info->m = p->m;
+  info->sigma = p->sigma;
+  info->window = p->prm.window;
+  info->precompute = p->prm.precompute;
+  info->lut_size = p->lut_size;
+  info->num_tiles = p->ntiles_total;
+  info->num_spread_tasks = p->n_tasks;
+  info->num_spread_entries = p->n_entries;
+  info->scratch_bytes = int64_t(p->scratch_bytes);
+  return NFFT_OK;
+}
+
+void* nfft_grid(nfft_plan* p) { return p ? p->grid : nullptr; }
+
+int nfft_get_timing(nfft_plan* p, double out[7]) {
+  if (!p || !out) return NFFT_ERR_INVALID_ARG;
+  NFFT_CUDA_TRY(cudaStreamSynchronize(p->stream));
+  for (int i = 0; i < 7; ++i) out[i] = p->timing[i];
+  return NFFT_OK;
+}
+
+int nfft_get_binning(nfft_plan* p, int32_t* perm, int32_t* tile_start, int32_t* grid_index) {
+  int rc = require_nodes(p);
+  if (rc) return rc;
+  const int64_t M = p->M, D = p->D;
+  NFFT_CUDA_TRY(cudaStreamSynchronize(p->stream));
+  std::vector<int32_t> hperm(M), hti(D * M);
+  if (M > 0) {
+    NFFT_CUDA_TRY(cudaMemcpy(hperm.data(), p->perm, sizeof(int32_t) * M, cudaMemcpyDeviceToHost));
+    NFFT_CUDA_TRY(cudaMemcpy(hti.data(), p->ti, sizeof(int32_t) * D * M, cudaMemcpyDeviceToHost));
+  }
+  if (perm && M > 0) std::memcpy(perm, hperm.data(), sizeof(int32_t) * M);
+  if (tile_start)
+    NFFT_CUDA_TRY(cudaMemcpy(tile_start, p->tile_start, sizeof(int32_t) * (p->ntiles_total + 1), cudaMemcpyDeviceToHost));
+  if (grid_index) {
+    for (int64_t i = 0; i < M; ++i)
+      for (int d = 0; d < D; ++d)
+        grid_index[d + D * int64_t(hperm[i])] = int32_t(wrap_any(hti[d * M + i] - p->m + 1, int(p->Nt[d])));
+  }
+  return NFFT_OK;
+}
+
+int nfft_get_deconv_factors(nfft_plan* p, void* out) {
+  if (!p || !out) return NFFT_ERR_INVALID_ARG;
+  const int64_t n = p->N[0] + (p->D > 1 ? p->N[1] : 0) + (p->D > 2 ? p->N[2] : 0);
+  NFFT_CUDA_TRY(cudaStreamSynchronize(p->stream));
+  NFFT_CUDA_TRY(cudaMemcpy(out, p->inv, p->real_size * n, cudaMemcpyDeviceToHost));
+  return NFFT_OK;
+}
+
+int nfft_sync(nfft_plan* p) {
+  if (!p) return NFFT_ERR_INVALID_ARG;
+  NFFT_CUDA_TRY(cudaStreamSynchronize(p->stream));
+  return NFFT_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,381 @@
+// Device precomputation of the plan: node checks, node reduction to grid
+// index + fractional offset, binning keys, deconvolution factors (FP64) and
+// the spreading task list.
+#include "nfft_internal.cuh"
+
+#include <math.h>
+
+namespace nfft {
+namespace {
+
+template <typename T>
+__global__ void check_nodes_kernel(const T* __restrict__ k, int64_t n, int* __restrict__ flag) {
+  int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  T x = k[i];
+  // checkNodes: !(abs(k) <= 0.5) also rejects NaN (src/utils.jl:46-55)
+  if (!(fabs(x) <= T(0.5))) atomicOr(flag, 1);
+}
+
+template <typename T>
+__global__ void reduce_nodes_kernel(const T* __restrict__ k, int D, int64_t M, int Nt0, int Nt1, int Nt2, int bs0,
+                                    int bs1, int bs2, int nt0, int nt1, int32_t* __restrict__ ti,
+                                    T* __restrict__ te, uint32_t* __restrict__ key, int32_t* __restrict__ val,
+                                    int32_t* __restrict__ tile_count) {
+  int64_t j = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (j >= M) return;
+  const int Nt[3] = {Nt0, Nt1, Nt2};
+  const int bs[3] = {bs0, bs1, bs2};
+  int b[3] = {0, 0, 0};
+  for (int d = 0; d < D; ++d) {
+    int32_t t;
+    T e;
+    reduce_coord<T>(k[int64_t(d) + int64_t(D) * j], Nt[d], t, e);
+    ti[int64_t(d) * M + j] = t;
+    te[int64_t(d) * M + j] = e;
+    b[d] = t / bs[d];
+  }
+  uint32_t kk = uint32_t(b[0] + nt0 * (b[1] + nt1 * b[2]));
+  key[j] = kk;
+  val[j] = int32_t(j);
+  atomicAdd(&tile_count[kk], 1);
+}
+
+template <typename T>
+__global__ void gather_sorted_kernel(const int32_t* __restrict__ perm, int D, int64_t M,
+                                     const int32_t* __restrict__ ti_u, const T* __restrict__ te_u,
+                                     int32_t* __restrict__ ti, T* __restrict__ te) {
+  int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= M) return;
+  const int64_t j = perm[i];
+  for (int d = 0; d < D; ++d) {
+    ti[int64_t(d) * M + i] = ti_u[int64_t(d) * M + j];
+    te[int64_t(d) * M + i] = te_u[int64_t(d) * M + j];
+  }
+}
+
+// ---------------------------------------------------------------- phi-hat
+
+__device__ double window_hat(int window, double n, double Nt, int m, double sigma) {
+  const double PI = 3.14159265358979323846;
+  switch (window) {
+    case NFFT_WINDOW_KAISER_BESSEL: {  // src/windowFunctions.jl:36-39
+      double b = PI * (2.0 - 1.0 / sigma);
+      double a = 2.0 * PI * n / Nt;
+      return bessel_i0_series<double>(m * sqrt(b * b - a * a));
+    }
+    case NFFT_WINDOW_GAUSS: {  // :70-73
+      double b = m / PI;
+      double a = PI * n / Nt;
+      return exp(-(a * a) * b);
+    }
+    case NFFT_WINDOW_SPLINE: {  // :98-100, Julia sinc(x) = sin(pi x)/(pi x)
+      double x = n / Nt;
+      double s = (x == 0.0) ? 1.0 : sin(PI * x) / (PI * x);
+      double r = 1.0;
+      for (int i = 0; i < 2 * m; ++i) r *= s;
+      return r;
+    }
+    case NFFT_WINDOW_KAISER_BESSEL_REV: {  // :51-57, real(sinc(sqrt(complex(a2))/pi))
+      double b = PI * (2.0 - 1.0 / sigma);
+      double u = 2.0 * PI * m * n / Nt;
+      double a2 = u * u - (m * b) * (m * b);
+      if (a2 > 0.0) {
+        double a = sqrt(a2);
+        return sin(a) / a;
+      } else if (a2 < 0.0) {
+        double a = sqrt(-a2);
+        return sinh(a) / a;
+      }
+      return 1.0;
+    }
+    case NFFT_WINDOW_COSH_TYPE: {  // :118-134
+      double beta = PI * m * (2.0 - 1.0 / sigma);
+      double gamma = beta / (2.0 * PI);
+      double zeta = PI / (cosh(beta) - 1.0) * m;
+      double arg = m * n / Nt;
+      double aa = fabs(arg);
+      double j0 = bessel_j0_series<double>(2.0 * PI * arg);
+      if (aa < gamma) {
+        double q = 2.0 * PI * arg;
+        return zeta * (bessel_i0_series<double>(sqrt(beta * beta - q * q)) - j0);
+      } else if (aa > gamma) {
+        double q = 2.0 * PI * arg;
+        return zeta * (bessel_j0_series<double>(sqrt(q * q - beta * beta)) - j0);
+      }
+      return zeta * (1.0 - bessel_j0_series<double>(beta));
+    }
+  }
+  return 1.0;
+}
+
+// precomputeWindowHatInvLUT (src/precomputation.jl:347-358), FP64: per
+// dimension a 30-point first-kind Chebyshev interpolant of
+// phi-hat(x + indexOffset(N)) on [1, N], evaluated at x = 1..N, inverted.
+// One CTA per dimension.
+template <typename T>
+__global__ void deconv_factors_kernel(int window, int m, double sigma, int D, int N0, int N1, int N2, int Nt0,
+                                      int Nt1, int Nt2, T* __restrict__ out) {
+  const int d = blockIdx.x;
+  if (d >= D) return;
+  const int Ns[3] = {N0, N1, N2};
+  const int Nts[3] = {Nt0, Nt1, Nt2};
+  const int N = Ns[d];
+  const double Nt = double(Nts[d]);
+  int offset = 0;
+  for (int q = 0; q < d; ++q) offset += Ns[q];
+  const double PI = 3.14159265358979323846;
+  const int ioff = -1 - N / 2;  // indexOffset, src/precomputation.jl:345
+  __shared__ double c[kChebNodes];
+  __shared__ double y[kChebNodes];
+  const double a = 1.0, b = double(N);
+  if (N > 1) {
+    for (int i = threadIdx.x; i < kChebNodes; i += blockDim.x) {
+      double th = PI * (2.0 * (i + 1) - 1.0) / (2.0 * kChebNodes);
+      double x = 0.5 * (b - a) * (cos(th) + 1.0) + a;
+      y[i] = window_hat(window, x + ioff, Nt, m, sigma);
+    }
+    __syncthreads();
+    for (int k = threadIdx.x; k < kChebNodes; k += blockDim.x) {
+      double s = 0.0;
+      for (int i = 0; i < kChebNodes; ++i) {
+        double th = PI * (2.0 * (i + 1) - 1.0) / (2.0 * kChebNodes);
+        s += y[i] * cos(k * th);
+      }
+      s *= 2.0 / kChebNodes;
+      c[k] = (k == 0) ? 0.5 * s : s;
+    }
+    __syncthreads();
+  }
+  for (int j = threadIdx.x; j < N; j += blockDim.x) {
+    double v;
+    if (N > 1) {
+      double t = (2.0 * (j + 1) - (a + b)) / (b - a);
+      double b1 = 0.0, b2 = 0.0;
+      for (int k = kChebNodes - 1; k >= 1; --k) {
+        double tmp = 2.0 * t * b1 - b2 + c[k];
+        b2 = b1;
+        b1 = tmp;
+      }
+      v = t * b1 - b2 + c[0];
+    } else {
+      v = window_hat(window, double(j + 1 + ioff), Nt, m, sigma);
+    }
+    out[offset + j] = T(1.0 / v);
+  }
+}
+
+// ------------------------------------------------------- spreading entries
+// Distinct tiles touched, in one dimension, by the taps t-m+1 .. t+m of a
+// node (wrapped).  Returns the count; ids in out[].
+__device__ __forceinline__ int tiles_touched(int t, int m, int Nt, int bs, int* out) {
+  int n = 0;
+  const int L = 2 * m;
+  for (int l = 0; l < L; ++l) {
+    int g = wrap_any(t - m + 1 + l, Nt);
+    int tile = g / bs;
+    bool seen = false;
+    for (int q = 0; q < n; ++q) seen |= (out[q] == tile);
+    if (!seen) out[n++] = tile;
+  }
+  return n;
+}
+
+__global__ void count_entries_kernel(const int32_t* __restrict__ ti, int D, int64_t M, int m, int Nt0, int Nt1,
+                                     int Nt2, int bs0, int bs1, int bs2, int32_t* __restrict__ ecount) {
+  int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= M) return;
+  const int Nt[3] = {Nt0, Nt1, Nt2};
+  const int bs[3] = {bs0, bs1, bs2};
+  int tl[kMaxL];
+  int c = 1;
+  for (int d = 0; d < D; ++d) c *= tiles_touched(ti[int64_t(d) * M + i], m, Nt[d], bs[d], tl);
+  ecount[i] = c;
+}
+
+__global__ void fill_entries_kernel(const int32_t* __restrict__ ti, int D, int64_t M, int m, int Nt0, int Nt1,
+                                    int Nt2, int bs0, int bs1, int bs2, int nt0, int nt1,
+                                    const int32_t* __restrict__ eoff, uint32_t* __restrict__ ekey,
+                                    int32_t* __restrict__ eval, int32_t* __restrict__ tcount) {
+  int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= M) return;
+  const int Nt[3] = {Nt0, Nt1, Nt2};
+  const int bs[3] = {bs0, bs1, bs2};
+  int tl[3][kMaxL];
+  int n[3] = {1, 1, 1};
+  tl[1][0] = 0;
+  tl[2][0] = 0;
+  for (int d = 0; d < D; ++d) n[d] = tiles_touched(ti[int64_t(d) * M + i], m, Nt[d], bs[d], tl[d]);
+  int pos = eoff[i];
+  for (int c = 0; c < n[2]; ++c)
+    for (int b = 0; b < n[1]; ++b)
+      for (int a = 0; a < n[0]; ++a) {
+        uint32_t tile = uint32_t(tl[0][a] + nt0 * (tl[1][b] + nt1 * tl[2][c]));
+        ekey[pos] = tile;
+        eval[pos] = int32_t(i);
+        atomicAdd(&tcount[tile], 1);
+        ++pos;
+      }
+}
+
+__global__ void task_counts_kernel(const int32_t* __restrict__ tstart, int64_t ntiles, int chunk,
+                                   int32_t* __restrict__ tcnt) {
+  int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (t >= ntiles) return;
+  int n = tstart[t + 1] - tstart[t];
+  tcnt[t] = n == 0 ? 1 : (n + chunk - 1) / chunk;
+}
+
+__global__ void fill_tasks_kernel(const int32_t* __restrict__ tstart, const int32_t* __restrict__ toff,
+                                  int64_t ntiles, int chunk, int4* __restrict__ tasks,
+                                  int32_t* __restrict__ multi, int* __restrict__ nmulti) {
+  int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (t >= ntiles) return;
+  const int s = tstart[t], e = tstart[t + 1];
+  const int n = e - s;
+  const int nc = n == 0 ? 1 : (n + chunk - 1) / chunk;
+  int pos = toff[t];
+  for (int c = 0; c < nc; ++c) {
+    int b = s + c * chunk;
+    int en = min(e, b + chunk);
+    tasks[pos + c] = make_int4(int(t), b, en, nc > 1 ? 1 : 0);
+  }
+  if (nc > 1) multi[atomicAdd(nmulti, 1)] = int(t);
+}
+
+}  // namespace
+
+template <typename T> static int check_nodes_t(const nfft_plan* p, const void* k, int* flag) {
+  const int64_t n = p->M * p->D;
+  if (n == 0) return NFFT_OK;
+  check_nodes_kernel<T><<<unsigned((n + 255) / 256), 256, 0, p->stream>>>(static_cast<const T*>(k), n, flag);
+  NFFT_LAUNCH_CHECK();
+  return NFFT_OK;
+}
+
+int launch_check_nodes(const nfft_plan* p, const void* k, int* flag) {
+  return p->precision == 32 ? check_nodes_t<float>(p, k, flag) : check_nodes_t<double>(p, k, flag);
+}
+
+template <typename T>
+static int reduce_t(const nfft_plan* p, const void* k, int32_t* ti_u, void* te_u, uint32_t* key, int32_t* val,
+                    int32_t* tile_count) {
+  if (p->M == 0) return NFFT_OK;
+  reduce_nodes_kernel<T><<<unsigned((p->M + 255) / 256), 256, 0, p->stream>>>(
+      static_cast<const T*>(k), p->D, p->M, int(p->Nt[0]), int(p->Nt[1]), int(p->Nt[2]), int(p->bs[0]),
+      int(p->bs[1]), int(p->bs[2]), int(p->ntiles[0]), int(p->ntiles[1]), ti_u, static_cast<T*>(te_u), key, val,
+      tile_count);
+  NFFT_LAUNCH_CHECK();
+  return NFFT_OK;
+}
+
+int launch_reduce_nodes(const nfft_plan* p, const void* k, int32_t* ti_u, void* te_u, uint32_t* key,
+                        int32_t* val, int32_t* tile_count) {
+  return p->precision == 32 ? reduce_t<float>(p, k, ti_u, te_u, key, val, tile_count)
+                            : reduce_t<double>(p, k, ti_u, te_u, key, val, tile_count);
+}
+
+template <typename T>
+static int gather_sorted_t(const nfft_plan* p, const int32_t* perm, const int32_t* ti_u, const void* te_u) {
+  if (p->M == 0) return NFFT_OK;
+  gather_sorted_kernel<T><<<unsigned((p->M + 255) / 256), 256, 0, p->stream>>>(
+      perm, p->D, p->M, ti_u, static_cast<const T*>(te_u), p->ti, static_cast<T*>(p->te));
+  NFFT_LAUNCH_CHECK();
+  return NFFT_OK;
+}
+
+int launch_gather_sorted(const nfft_plan* p, const int32_t* perm, const int32_t* ti_u, const void* te_u) {
+  return p->precision == 32 ? gather_sorted_t<float>(p, perm, ti_u, te_u)
+                            : gather_sorted_t<double>(p, perm, ti_u, te_u);
+}
+
+int launch_deconv_factors(nfft_plan* p) {
+  if (p->precision == 32) {
+    deconv_factors_kernel<float><<<p->D, 128, 0, p->stream>>>(
+        p->prm.window, p->m, p->sigma, p->D, int(p->N[0]), int(p->N[1]), int(p->N[2]), int(p->Nt[0]),
+        int(p->Nt[1]), int(p->Nt[2]), static_cast<float*>(p->inv));
+  } else {
+    deconv_factors_kernel<double><<<p->D, 128, 0, p->stream>>>(
+        p->prm.window, p->m, p->sigma, p->D, int(p->N[0]), int(p->N[1]), int(p->N[2]), int(p->Nt[0]),
+        int(p->Nt[1]), int(p->Nt[2]), static_cast<double*>(p->inv));
+  }
+  NFFT_LAUNCH_CHECK();
+  return NFFT_OK;
+}
+
+int launch_count_entries(const nfft_plan* p, int32_t* ecount) {
+  if (p->M == 0) return NFFT_OK;
+  count_entries_kernel<<<unsigned((p->M + 255) / 256), 256, 0, p->stream>>>(
+      p->ti, p->D, p->M, p->m, int(p->Nt[0]), int(p->Nt[1]), int(p->Nt[2]), int(p->bs[0]), int(p->bs[1]),
+      int(p->bs[2]), ecount);
+  NFFT_LAUNCH_CHECK();
+  return NFFT_OK;
+}
+
+int launch_fill_entries(const nfft_plan* p, const int32_t* eoff, uint32_t* ekey, int32_t* eval, int32_t* tcount) {
+  if (p->M == 0) return NFFT_OK;
+  fill_entries_kernel<<<unsigned((p->M + 255) / 256), 256, 0, p->stream>>>(
+      p->ti, p->D, p->M, p->m, int(p->Nt[0]), int(p->Nt[1]), int(p->Nt[2]), int(p->bs[0]), int(p->bs[1]),
+      int(p->bs[2]), int(p->ntiles[0]), int(p->ntiles[1]), eoff, ekey, eval, tcount);
+  NFFT_LAUNCH_CHECK();
+  return NFFT_OK;
+}
+
+// Chunk the tiles' entry ranges into spreading tasks.  tile_estart holds
+// ntiles+1 offsets on the device.  Allocates p->tasks and p->multi_tiles.
+int launch_build_tasks(nfft_plan* p, const int32_t* tile_estart, int chunk) {
+  const int64_t nt = p->ntiles_total;
+  int32_t *tcnt = nullptr, *toff = nullptr;
+  void* scr = nullptr;
+  int* nmulti = nullptr;
+  int rc = NFFT_OK;
+  const size_t sb = scan_scratch_bytes(nt + 1);
+  if (cudaMalloc(&tcnt, sizeof(int32_t) * (nt + 1)) != cudaSuccess ||
+      cudaMalloc(&toff, sizeof(int32_t) * (nt + 1)) != cudaSuccess || cudaMalloc(&scr, sb) != cudaSuccess ||
+      cudaMalloc(&nmulti, sizeof(int)) != cudaSuccess) {
+    set_error("cudaMalloc failed while building spreading tasks");
+    rc = NFFT_ERR_ALLOC;
+  }
+  int32_t ntasks = 0, nm = 0;
+  if (!rc) {
+    task_counts_kernel<<<unsigned((nt + 255) / 256), 256, 0, p->stream>>>(tile_estart, nt, chunk, tcnt);
+    g_launches.fetch_add(1);
+    cudaMemsetAsync(tcnt + nt, 0, sizeof(int32_t), p->stream);
+    rc = exclusive_scan_i32(tcnt, toff, nt + 1, scr, sb, p->stream);
+  }
+  if (!rc) {
+    cudaMemcpyAsync(&ntasks, toff + nt, sizeof(int32_t), cudaMemcpyDeviceToHost, p->stream);
+    if (cudaStreamSynchronize(p->stream) != cudaSuccess) {
+      set_error("stream sync failed while building spreading tasks");
+      rc = NFFT_ERR_CUDA;
+    }
+  }
+  if (!rc) {
+    p->n_tasks = ntasks;
+    if (cudaMalloc(&p->tasks, sizeof(int4) * size_t(ntasks > 0 ? ntasks : 1)) != cudaSuccess ||
+        cudaMalloc(&p->multi_tiles, sizeof(int32_t) * size_t(nt > 0 ? nt : 1)) != cudaSuccess) {
+      set_error("cudaMalloc failed for spreading tasks");
+      rc = NFFT_ERR_ALLOC;
+    }
+  }
+  if (!rc) {
+    p->scratch_bytes += sizeof(int4) * size_t(ntasks) + sizeof(int32_t) * size_t(nt);
+    cudaMemsetAsync(nmulti, 0, sizeof(int), p->stream);
+    fill_tasks_kernel<<<unsigned((nt + 255) / 256), 256, 0, p->stream>>>(tile_estart, toff, nt, chunk, p->tasks,
+                                                                         p->multi_tiles, nmulti);
+    g_launches.fetch_add(1);
+    cudaMemcpyAsync(&nm, nmulti, sizeof(int), cudaMemcpyDeviceToHost, p->stream);
+    if (cudaStreamSynchronize(p->stream) != cudaSuccess || cudaGetLastError() != cudaSuccess) {
+      set_error("building spreading tasks failed");
+      rc = NFFT_ERR_CUDA;
+    }
+    p->n_multi = nm;
+  }
+  cudaFree(tcnt);
+  cudaFree(toff);
+  cudaFree(scr);
+  cudaFree(nmulti);
+  return rc;
+}
+
+}  // namespace nfft

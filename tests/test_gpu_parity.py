@@ -1,0 +1,140 @@
+"""GPU parity: the CUDA plan through the C ABI against the oracle (CPU
+restatement of NFFT.jl) and against the direct NDFT (src/direct.jl).
+
+Tolerances: FP64 path rel l2 <= 1e-11 against the FP64 oracle on identical
+inputs; FP32 path rel l2 <= 1e-5; integer work (bins, sort permutation, grid
+indices) bit-exact; NDFT tolerances per window as in test/accuracy.jl:46 and
+test/gpu.jl:22.
+"""
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+import nfftgb300 as nf  # noqa: E402
+from oracle import oracle  # noqa: E402
+
+TOL64 = 1e-11
+TOL32 = 1e-5
+
+
+def rand_problem(D, N, M, seed, dtype=np.float64):
+    rng = np.random.default_rng(seed)
+    k = (rng.random((D, M)) - 0.5).astype(dtype)
+    f = (rng.standard_normal(N) + 1j * rng.standard_normal(N)) / np.sqrt(2)
+    fhat = (rng.standard_normal(M) + 1j * rng.standard_normal(M)) / np.sqrt(2)
+    return k, f, fhat
+
+
+def gpu_fwd_adj(p, f, fhat):
+    cd = p.cdtype
+    y = (p * nf.as_colmajor(f, p.N, cd)).cpu().numpy()
+    x = nf.adjoint(p) * torch.as_tensor(fhat).to(cd)
+    x = x.cpu().numpy()
+    return y, x
+
+
+def colmajor_flat(x):
+    return np.asarray(x).ravel(order="F")
+
+
+CASES = [
+    (1, (64,), 200),
+    (1, (255,), 255),
+    (2, (16, 16), 300),
+    (2, (31, 33), 1023),
+    (3, (8, 8, 8), 400),
+    (3, (11, 12, 14), 1848),
+]
+
+
+@pytest.mark.parametrize("D,N,M", CASES)
+@pytest.mark.parametrize("pre", [oracle.TENSOR, oracle.LINEAR, oracle.FULL])
+def test_fp64_matches_oracle(D, N, M, pre):
+    k, f, fhat = rand_problem(D, N, M, seed=123 + D)
+    for m in (4, 5):
+        p = nf.plan_nfft(k, N, m=m, sigma=2.0, precompute=pre)
+        op = oracle.OraclePlan(k, N, m=m, sigma=2.0, precompute=pre)
+        y, x = gpu_fwd_adj(p, f, fhat)
+        assert oracle.rel_l2(y, op.forward(f)) < TOL64
+        assert oracle.rel_l2(colmajor_flat(x), colmajor_flat(op.adjoint(fhat))) < TOL64
+
+
+@pytest.mark.parametrize("D,N,M", CASES)
+def test_fp32_matches_oracle(D, N, M):
+    k, f, fhat = rand_problem(D, N, M, seed=7 + D, dtype=np.float32)
+    p = nf.plan_nfft(k, N, m=4, sigma=2.0)
+    op64 = oracle.OraclePlan(k.astype(np.float64), N, m=4, sigma=2.0)
+    op32 = oracle.OraclePlan(k, N, m=4, sigma=2.0, dtype=np.float32)
+    y, x = gpu_fwd_adj(p, f, fhat)
+    y64 = op64.forward(f)
+    x64 = colmajor_flat(op64.adjoint(fhat))
+    assert oracle.rel_l2(y, y64) < TOL32
+    assert oracle.rel_l2(colmajor_flat(x), x64) < TOL32
+    assert oracle.rel_l2(y, op32.forward(f.astype(np.complex64))) < TOL32
+    assert oracle.rel_l2(colmajor_flat(x), colmajor_flat(op32.adjoint(fhat.astype(np.complex64)))) < TOL32
+
+
+WINDOWS = [("kaiser_bessel", 1e-7), ("gauss", 1e-3), ("kaiser_bessel_rev", 1e-6), ("spline", 1e-4),
+           ("cosh_type", 1e-7)]
+
+
+@pytest.mark.parametrize("N", [(256,), (32, 32), (12, 12, 12)])
+@pytest.mark.parametrize("window,eps", WINDOWS)
+@pytest.mark.parametrize("pre", [oracle.FULL, oracle.TENSOR])
+def test_accuracy_vs_ndft(N, window, eps, pre):
+    """test/gpu.jl:17-50 and test/accuracy.jl:41-73: m=5, sigma=2, J=|N|."""
+    D = len(N)
+    J = int(np.prod(N))
+    rng = np.random.default_rng(42)
+    k = rng.random((D, J)) - 0.5
+    fhat = rng.random(J) + 1j * rng.random(J)
+    p = nf.plan_nfft(k, N, m=5, sigma=2.0, window=window, precompute=pre)
+    f = oracle.ndft_adjoint(k, N, fhat)
+    fa = (nf.adjoint(p) * torch.as_tensor(fhat)).cpu().numpy()
+    assert oracle.rel_l2(colmajor_flat(fa), colmajor_flat(f)) < eps
+    g = oracle.ndft_forward(k, f)
+    ga = (p * nf.as_colmajor(f, N, torch.complex128)).cpu().numpy()
+    assert oracle.rel_l2(ga, g) < eps
+
+
+@pytest.mark.parametrize("D,N,M", [(1, (512,), 3000), (2, (64, 48), 5000), (3, (16, 20, 12), 6000)])
+def test_binning_bit_exact(D, N, M):
+    """Bins, stable sort permutation and grid indices equal the oracle's
+    blocking (src/precomputation.jl:487-520) bit for bit, with the reference's
+    default block sizes, for FP64 and FP32 nodes."""
+    for dtype in (np.float64, np.float32):
+        k, _, _ = rand_problem(D, N, M, seed=99, dtype=dtype)
+        # nodes exactly on grid lines and on the [-0.5, 0.5] boundary
+        k[:, :10] = (np.arange(10) / 20.0 - 0.25).astype(dtype)
+        k[0, 10] = -0.5
+        k[-1, 11] = 0.5
+        k[0, 12] = -np.finfo(dtype).tiny
+        op = oracle.OraclePlan(k, N, m=4, sigma=2.0, dtype=dtype)
+        ob = op.blocks()
+        p = nf.plan_nfft(k, N, m=4, sigma=2.0, blockSize=op.block_size)
+        gb = p.binning()
+        assert np.array_equal(gb["perm"], ob["nodes"])
+        assert np.array_equal(gb["tile_start"], ob["block_start"])
+        Nt = np.array(op.Nt)[:, None]
+        assert np.array_equal(gb["grid_index"], (ob["trunc"] - 4 + 1) % Nt)
+
+
+def test_deconv_factors_match_oracle():
+    for N in [(64,), (31, 33), (11, 12, 14)]:
+        for window in ("kaiser_bessel", "gauss", "spline", "kaiser_bessel_rev", "cosh_type"):
+            p = nf.plan_nfft(np.zeros((len(N), 3)), N, m=5, sigma=2.0, window=window)
+            ref = oracle.deconv_factors(window, N, p.Ñ, 5, 2.0)
+            for a, b in zip(p.deconv_factors(), ref):
+                assert np.max(np.abs(a - b) / np.abs(b)) < 1e-12
+
+
+def test_plain_path_matches_oracle():
+    for D, N, M in [(1, (128,), 500), (2, (24, 20), 700), (3, (10, 8, 12), 900)]:
+        k, f, fhat = rand_problem(D, N, M, seed=5)
+        p = nf.plan_nfft(k, N, m=4, sigma=2.0, blocking=False)
+        op = oracle.OraclePlan(k, N, m=4, sigma=2.0)
+        y, x = gpu_fwd_adj(p, f, fhat)
+        assert oracle.rel_l2(y, op.forward(f)) < TOL64
+        assert oracle.rel_l2(colmajor_flat(x), colmajor_flat(op.adjoint(fhat))) < TOL64
