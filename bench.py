@@ -1,0 +1,416 @@
+"""Benchmark: forward + adjoint NFFT throughput on the 3-D radial ("koosh-ball")
+workload, N = 256^3, 8192 spokes x 512 samples (M = 4,194,304 nodes), FP32,
+Kaiser-Bessel window, m = 4, sigma = 2.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+A step is one forward NFFT (mul!(fHat, p, f)) plus one adjoint NFFT
+(mul!(f, adjoint(p), fHat)) over the whole node set.  value = nodes/s over
+the timed steps with inputs resident in HBM; e2e = the same through the
+C-ABI calls with the inputs copied from pinned host memory and the results
+copied back inside the timed region.  The inputs (1.07 GB oversampled grid,
+134 MB image) are larger than L2, so no extra L2 flush is done.
+
+--impl reference times the oracle, the CPU restatement of NFFT.jl's blocked
+algorithm (FFT: scipy/pocketfft), on the host cores with all threads.
+Under torchrun each rank runs an independent replica (the plan does not
+shard); value is the aggregate over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+for _p in (ROOT, os.path.join(ROOT, "nfft.jl_gb300")):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+METRIC = "fwd+adj NFFT nodes/s @256^3 FP32 (<=1e-5 vs FP64 NDFT) vs plain path; HBM GB/s"
+UNIT = "nodes/s"
+N3 = (256, 256, 256)
+SPOKES, SAMPLES = 8192, 512
+M_NODES = SPOKES * SAMPLES
+WORKLOAD = "3D radial koosh-ball NFFT fwd+adj, N=256^3, 8192 spokes x 512 samples (M=4194304), KB m=4 sigma=2"
+# DRAM bytes (read + write) per launch of the spreading kernel from one ncu
+# capture (profiles/spread_tile_radial256.md); None until measured.
+SPREAD_DRAM_BYTES = None
+
+
+def radial_nodes(dtype=np.float32):
+    """Spoke directions on a golden-angle (Fibonacci) spiral over the
+    hemisphere, z_i = (i + 1/2)/8192, phi_i = i*pi*(3 - sqrt 5); samples at
+    radius r_s = -1/2 + s/512, s = 0..511.  Returns k of shape (3, M)."""
+    i = np.arange(SPOKES, dtype=np.float64)
+    z = (i + 0.5) / SPOKES
+    ph = i * math.pi * (3.0 - math.sqrt(5.0))
+    rxy = np.sqrt(1.0 - z * z)
+    u = np.stack([rxy * np.cos(ph), rxy * np.sin(ph), z])  # (3, spokes)
+    r = -0.5 + np.arange(SAMPLES, dtype=np.float64) / SAMPLES
+    k = (u[:, :, None] * r[None, None, :]).reshape(3, -1)
+    return np.clip(k, -0.5, 0.5).astype(dtype)
+
+
+def complex_normal(rng, shape, dtype=np.complex64):
+    return ((rng.standard_normal(shape) + 1j * rng.standard_normal(shape)) / math.sqrt(2)).astype(dtype)
+
+
+def measured_peak_hbm():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as fh:
+            return float(json.load(fh)["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle samples during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index=0):
+        self.proc = None
+        self.gpu_index = gpu_index
+        self.out = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu_index}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self._t = threading.Thread(target=self._read, daemon=True)
+            self._t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.out.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+            self._t.join(timeout=2)
+
+    def summary(self):
+        if not self.out:
+            return None
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.out:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = float(parts[2])
+            except ValueError:
+                continue
+            for nm, val in zip(names, parts[5:9]):
+                if val.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def rel_err_subset(k64, f, fhat, y, x, n_fwd=48, n_adj=24, seed=7):
+    """Relative l2 errors of the GPU outputs on node / frequency subsets
+    against the FP64 NDFT (oracle)."""
+    from oracle import oracle
+    rng = np.random.default_rng(seed)
+    M = k64.shape[1]
+    sub = rng.choice(M, n_fwd, replace=False)
+    ref_y = oracle.ndft_forward(k64, f, subset=sub)
+    e_fwd = oracle.rel_l2(y[sub], ref_y)
+    N = f.shape
+    lin = rng.choice(int(np.prod(N)), n_adj, replace=False)
+    ref_x = oracle.ndft_adjoint(k64, N, fhat, subset=lin)
+    e_adj = oracle.rel_l2(x.ravel(order="F")[lin], ref_x)
+    return e_fwd, e_adj
+
+
+def cpu_reference_run(steps, warmup, budget_s=150.0):
+    """The oracle (FP32) on the host cores: full forward + adjoint steps."""
+    from oracle import oracle
+    lib = oracle.lib()
+    threads = lib.oracle_num_threads()
+    k = radial_nodes(np.float32)
+    rng = np.random.default_rng(123)
+    f = complex_normal(rng, N3)
+    fhat = complex_normal(rng, M_NODES)
+    p = oracle.OraclePlan(k, N3, m=4, sigma=2.0, window="kaiser_bessel", precompute=oracle.TENSOR,
+                          dtype=np.float32, fft_workers=threads)
+    t_start = time.perf_counter()
+    times = []
+    done_w = 0
+    for it in range(warmup + steps):
+        t0 = time.perf_counter()
+        p.forward(f)
+        p.adjoint(fhat)
+        dt = time.perf_counter() - t0
+        if it < warmup:
+            done_w += 1
+        else:
+            times.append(dt)
+        elapsed = time.perf_counter() - t_start
+        if times and elapsed + dt > budget_s and len(times) >= 1:
+            break
+    per = statistics.median(times)
+    return {"value": M_NODES / per, "seconds_per_step": per, "steps": len(times), "warmup": done_w,
+            "cores": threads,
+            "sample": f"full workload (M={M_NODES}, 256^3, FP32), {len(times)} timed fwd+adj pairs; "
+                      f"oracle restatement of NFFT.jl blocked TENSOR, FFT via scipy.fft workers={threads}"}
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    r = cpu_reference_run(args.steps, args.warmup)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": r["value"], "unit": UNIT, "n_gpus": args.gpus,
+        "steps": r["steps"], "warmup": r["warmup"], "ms_per_step": r["seconds_per_step"] * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "precision": "FP32", "parallelism": "host threads"},
+        "cpu_baseline": {"value": r["value"], "unit": UNIT, "cores": r["cores"], "kind": "port",
+                         "sample": r["sample"]},
+        "e2e": {"value": r["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_ours(args):
+    import torch
+    import torch.distributed as dist
+    import nfftgb300 as nf
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    dev = torch.device("cuda", torch.cuda.current_device())
+
+    k = radial_nodes(np.float32)
+    rng = np.random.default_rng(123)
+    f_h = complex_normal(rng, N3)
+    fhat_h = complex_normal(rng, M_NODES)
+
+    # ---- FP32 tiled plan (the product path)
+    stats = nf.TimingStats()
+    t0 = time.perf_counter()
+    p = nf.plan_nfft(k, N3, m=4, sigma=2.0, window="kaiser_bessel", precompute=nf.POLYNOMIAL, timing=stats)
+    torch.cuda.synchronize()
+    t_pre = time.perf_counter() - t0
+    f = nf.as_colmajor(f_h, N3, torch.complex64, dev)
+    fhat = torch.from_numpy(fhat_h).to(dev)
+    y = torch.empty(M_NODES, dtype=torch.complex64, device=dev)
+    x = nf.empty_image(N3, torch.complex64, dev)
+    lib = nf.load()
+
+    def step():
+        p.forward_(y, f)
+        p.adjoint_(x, fhat)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    lib.nfft_timing_reset(p._handle)
+    launches0 = nf.kernel_launch_count()
+    stream = torch.cuda.current_stream(dev)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        if world > 1:
+            dist.barrier()
+        torch.cuda.synchronize()
+        ev0.record(stream)
+        for _ in range(args.steps):
+            step()
+        ev1.record(stream)
+        torch.cuda.synchronize()
+        if world > 1:
+            dist.barrier()
+    launches = nf.kernel_launch_count() - launches0
+    t_dev = ev0.elapsed_time(ev1) * 1e-3
+    if world > 1:
+        tt = torch.tensor([t_dev], device=dev, dtype=torch.float64)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t_dev = float(tt.item())
+    value = world * M_NODES * args.steps / t_dev
+
+    import ctypes
+    tot = (ctypes.c_double * 7)()
+    calls = (ctypes.c_int64 * 2)()
+    lib.nfft_get_timing_totals(p._handle, tot, calls)
+    nf_ = max(calls[0], 1)
+    na_ = max(calls[1], 1)
+    stages = {"deconv_pad_ms": tot[3] / nf_ * 1e3, "fft_fwd_ms": tot[2] / nf_ * 1e3, "gather_ms": tot[1] / nf_ * 1e3,
+              "spread_ms": tot[4] / na_ * 1e3, "fft_adj_ms": tot[5] / na_ * 1e3, "crop_ms": tot[6] / na_ * 1e3}
+
+    # ---- e2e through the C-ABI with pinned host buffers
+    f_pin = torch.from_numpy(np.ascontiguousarray(f_h.ravel(order="F"))).pin_memory()
+    fhat_pin = torch.from_numpy(fhat_h).pin_memory()
+    y_pin = torch.empty(M_NODES, dtype=torch.complex64).pin_memory()
+    x_pin = torch.empty(int(np.prod(N3)), dtype=torch.complex64).pin_memory()
+    f_dev_flat = torch.empty(int(np.prod(N3)), dtype=torch.complex64, device=dev)
+    fhat_dev = torch.empty(M_NODES, dtype=torch.complex64, device=dev)
+    f_dev = f_dev_flat.reshape(N3[::-1]).permute(2, 1, 0)
+    x_flat = x.permute(2, 1, 0).reshape(-1)
+
+    def e2e_step():
+        f_dev_flat.copy_(f_pin, non_blocking=True)
+        fhat_dev.copy_(fhat_pin, non_blocking=True)
+        p.forward_(y, f_dev)
+        p.adjoint_(x, fhat_dev)
+        y_pin.copy_(y, non_blocking=True)
+        x_pin.copy_(x_flat, non_blocking=True)
+
+    for _ in range(max(1, args.warmup // 2)):
+        e2e_step()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e2e_steps = max(3, args.steps // 2)
+    if world > 1:
+        dist.barrier()
+    e0.record(stream)
+    for _ in range(e2e_steps):
+        e2e_step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    t_e2e = e0.elapsed_time(e1) * 1e-3
+    if world > 1:
+        tt = torch.tensor([t_e2e], device=dev, dtype=torch.float64)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t_e2e = float(tt.item())
+    e2e_value = world * M_NODES * e2e_steps / t_e2e
+    h2d = f_pin.numel() * 8 + fhat_pin.numel() * 8
+    d2h = y_pin.numel() * 8 + x_pin.numel() * 8
+
+    # ---- accuracy of this run's outputs (outside the timed region)
+    err_fwd = err_adj = None
+    if rank == 0 and not args.no_check:
+        p.forward_(y, f)
+        p.adjoint_(x, fhat)
+        err_fwd, err_adj = rel_err_subset(k.astype(np.float64), f_h.astype(np.complex128),
+                                          fhat_h.astype(np.complex128), y.cpu().numpy(),
+                                          x.cpu().numpy())
+
+    # ---- the plain FP64 path on the same workload (comparator)
+    plain = None
+    if not args.no_plain:
+        k64 = k.astype(np.float64)
+        pp = nf.plan_nfft(k64, N3, m=4, sigma=2.0, window="kaiser_bessel", precompute=nf.POLYNOMIAL,
+                          blocking=False)
+        f64 = f.to(torch.complex128)
+        fhat64 = fhat.to(torch.complex128)
+        y64 = torch.empty(M_NODES, dtype=torch.complex128, device=dev)
+        x64 = nf.empty_image(N3, torch.complex128, dev)
+        pp.forward_(y64, f64)
+        pp.adjoint_(x64, fhat64)
+        torch.cuda.synchronize()
+        q0, q1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        nplain = 3
+        q0.record(stream)
+        for _ in range(nplain):
+            pp.forward_(y64, f64)
+            pp.adjoint_(x64, fhat64)
+        q1.record(stream)
+        torch.cuda.synchronize()
+        t_plain = q0.elapsed_time(q1) * 1e-3
+        plain = {"value": M_NODES * nplain / t_plain, "unit": UNIT, "ms_per_step": t_plain / nplain * 1e3,
+                 "speedup_of_value": value / world / (M_NODES * nplain / t_plain)}
+        del pp, f64, fhat64, y64, x64
+        torch.cuda.empty_cache()
+
+    # ---- roofline of the dominant kernel of this library
+    peak, peak_kind = measured_peak_hbm()
+    s_r, s_c, D = 4, 8, 3
+    ng = int(np.prod([2 * n for n in N3]))
+    nimg = int(np.prod(N3))
+    alg = {
+        "spread_ms": M_NODES * (D * s_r + s_c) + ng * s_c,
+        "gather_ms": ng * s_c + M_NODES * (D * s_r + s_c),
+        "deconv_pad_ms": nimg * s_c + ng * s_c,
+        "crop_ms": 2 * nimg * s_c,
+    }
+    dom = max(alg, key=lambda s: stages[s])
+    t_dom = stages[dom] * 1e-3
+    achieved = alg[dom] / t_dom / 1e9
+    kernel_names = {"spread_ms": "spread_tile_kernel", "gather_ms": "interp_warp_kernel",
+                    "deconv_pad_ms": "pad_apodize_kernel", "crop_ms": "crop_apodize_kernel"}
+    roofline = {"bound": "hbm", "kernel": kernel_names[dom], "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "peak_source": f"{peak_kind} hbm_gbs",
+                "algorithmic_bytes": alg[dom],
+                "traffic": SPREAD_DRAM_BYTES if dom == "spread_ms" else None}
+    pair_bytes = 7 * ng * s_c + 3 * nimg * s_c + 2 * M_NODES * (D * s_r + s_c)
+    pair_gbs = pair_bytes * args.steps / (t_dev / world * world) / 1e9 if False else pair_bytes / (t_dev / args.steps) / 1e9
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        r = cpu_reference_run(steps=1, warmup=0, budget_s=60.0)
+        cpu = {"value": r["value"], "unit": UNIT, "cores": r["cores"], "kind": "port", "sample": r["sample"]}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": t_dev / args.steps * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "precision": "FP32 (FP64 node reduction and deconvolution factors)",
+                       "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
+                       "l2": "inputs larger than L2 (grid 1.07 GB, image 134 MB); no extra flush",
+                       "plan_seconds": t_pre},
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                    "steps": e2e_steps},
+            "gpu_launches": int(launches),
+            "roofline": roofline,
+            "pair_hbm_gbs": pair_gbs,
+            "stages_ms": stages,
+            "rel_err_vs_fp64_ndft": {"forward": err_fwd, "adjoint": err_adj},
+            "plain_fp64_path": plain,
+            "cpu_baseline": cpu,
+            "clocks": clk.summary(),
+        }
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-plain", action="store_true")
+    ap.add_argument("--no-check", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -78,7 +78,7 @@ enum { NFFT_F32 = 32, NFFT_F64 = 64 };
  * before calling. */
 typedef struct {
   int32_t m;                /* window half width (taps per dimension: 2m), 2..8 */
-  double sigma;             /* oversampling factor; Ntilde = 2*ceil(sigma*N/2) */
+  double sigma;             /* oversampling factor; Ntilde = (ceil(sigma*N) / 2) * 2 */
   int32_t window;           /* NFFT_WINDOW_* */
   int32_t precompute;       /* NFFT_PRECOMPUTE_* */
   int32_t blocking;         /* 1: bin-sorted tiled kernels; 0: per-node kernels
@@ -187,6 +187,14 @@ void* nfft_grid(nfft_plan* plan);
  * transforms as {pre, conv, fft, deconv, conv_adjoint, fft_adjoint,
  * deconv_adjoint}.  Synchronises the stream. */
 int nfft_get_timing(nfft_plan* plan, double out[7]);
+
+/* Stage totals over all transforms since the last nfft_timing_reset (same
+ * order as nfft_get_timing, pre excluded) and the number of forward
+ * (calls[0]) and adjoint (calls[1]) transforms they cover.  Synchronises. */
+int nfft_get_timing_totals(nfft_plan* plan, double totals[7], int64_t calls[2]);
+
+/* Clear the stage totals. */
+int nfft_timing_reset(nfft_plan* plan);
 
 /* Integer outputs of the binning, copied to host buffers (the reference's
  * nodesInBlock, src/precomputation.jl:487-520): perm[i] = node at sorted

@@ -116,9 +116,17 @@ struct nfft_plan {
   int* dflag = nullptr;            // device status word
   size_t scratch_bytes = 0;
 
+  // TimingStats: every forward/adjoint records 4 events into a ring slot; the
+  // slots are harvested (summed per stage) lazily, so timing adds no host
+  // synchronisation to the calls themselves.
   bool timing_on = false;
-  cudaEvent_t ev[4] = {};
-  double timing[7] = {};
+  static constexpr int kRing = 64;
+  cudaEvent_t ev[kRing][4] = {};
+  int ring_dir[kRing] = {};        // -1 empty, 0 forward, 1 adjoint
+  int64_t ring_next = 0;
+  double timing[7] = {};           // last call per stage (seconds)
+  double timing_sum[7] = {};       // totals since the last reset
+  int64_t timing_calls[2] = {0, 0};
 };
 
 namespace nfft {

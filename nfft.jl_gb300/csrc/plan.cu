@@ -194,26 +194,48 @@ int exec_fft(nfft_plan* p, int dir) {
   return cufft_check(cufftExecZ2Z(p->fft, g, g, dir), "exec");
 }
 
-void record(nfft_plan* p, int i) {
-  if (p->timing_on) cudaEventRecord(p->ev[i], p->stream);
+// Harvest one ring slot (waits for its last event).
+void harvest(nfft_plan* p, int slot) {
+  const int dir = p->ring_dir[slot];
+  if (dir < 0) return;
+  cudaEventSynchronize(p->ev[slot][3]);
+  float a = 0, b = 0, c = 0;
+  cudaEventElapsedTime(&a, p->ev[slot][0], p->ev[slot][1]);
+  cudaEventElapsedTime(&b, p->ev[slot][1], p->ev[slot][2]);
+  cudaEventElapsedTime(&c, p->ev[slot][2], p->ev[slot][3]);
+  // forward: deconv, fft, conv; adjoint: conv, fft, deconv
+  const int ia = dir == 0 ? 3 : 4, ib = dir == 0 ? 2 : 5, ic = dir == 0 ? 1 : 6;
+  p->timing[ia] = a * 1e-3;
+  p->timing[ib] = b * 1e-3;
+  p->timing[ic] = c * 1e-3;
+  p->timing_sum[ia] += a * 1e-3;
+  p->timing_sum[ib] += b * 1e-3;
+  p->timing_sum[ic] += c * 1e-3;
+  p->timing_calls[dir] += 1;
+  p->ring_dir[slot] = -1;
 }
 
-void collect_timing(nfft_plan* p, int base) {
+void harvest_all(nfft_plan* p) {
   if (!p->timing_on) return;
-  cudaEventSynchronize(p->ev[3]);
-  float a = 0, b = 0, c = 0;
-  cudaEventElapsedTime(&a, p->ev[0], p->ev[1]);
-  cudaEventElapsedTime(&b, p->ev[1], p->ev[2]);
-  cudaEventElapsedTime(&c, p->ev[2], p->ev[3]);
-  if (base == 0) {  // forward: deconv, fft, conv
-    p->timing[3] = a * 1e-3;
-    p->timing[2] = b * 1e-3;
-    p->timing[1] = c * 1e-3;
-  } else {  // adjoint: conv, fft, deconv
-    p->timing[4] = a * 1e-3;
-    p->timing[5] = b * 1e-3;
-    p->timing[6] = c * 1e-3;
-  }
+  // oldest first so that timing[] ends with the latest call
+  for (int q = 0; q < nfft_plan::kRing; ++q) harvest(p, int((p->ring_next + q) % nfft_plan::kRing));
+}
+
+// Slot for the next call; a full ring is harvested first.
+int ring_slot(nfft_plan* p) {
+  const int slot = int(p->ring_next % nfft_plan::kRing);
+  if (p->ring_dir[slot] >= 0) harvest(p, slot);
+  return slot;
+}
+
+void record(nfft_plan* p, int slot, int i) {
+  if (p->timing_on) cudaEventRecord(p->ev[slot][i], p->stream);
+}
+
+void finish_record(nfft_plan* p, int slot, int dir) {
+  if (!p->timing_on) return;
+  p->ring_dir[slot] = dir;
+  p->ring_next += 1;
 }
 
 }  // namespace
@@ -402,7 +424,10 @@ int nfft_plan_create(nfft_plan** out, int precision, int D, const int64_t* N, in
   if (rc) return fail(rc);
   if (prm.timing) {
     p->timing_on = true;
-    for (int i = 0; i < 4; ++i) cudaEventCreate(&p->ev[i]);
+    for (int s = 0; s < nfft_plan::kRing; ++s) {
+      p->ring_dir[s] = -1;
+      for (int i = 0; i < 4; ++i) cudaEventCreate(&p->ev[s][i]);
+    }
   }
   if (cudaStreamSynchronize(p->stream) != cudaSuccess || cudaGetLastError() != cudaSuccess) {
     set_error("plan construction failed on the device");
@@ -423,7 +448,8 @@ int nfft_plan_destroy(nfft_plan* p) {
   cudaFree(p->cbuf);
   if (p->fft_ok) cufftDestroy(p->fft);
   if (p->timing_on)
-    for (int i = 0; i < 4; ++i) cudaEventDestroy(p->ev[i]);
+    for (int s = 0; s < nfft_plan::kRing; ++s)
+      for (int i = 0; i < 4; ++i) cudaEventDestroy(p->ev[s][i]);
   delete p;
   return NFFT_OK;
 }
@@ -587,34 +613,36 @@ static int require_nodes(const nfft_plan* p) {
 int nfft_forward(nfft_plan* p, const void* f, void* fhat) {
   int rc = require_nodes(p);
   if (rc) return rc;
-  record(p, 0);
+  const int slot = p->timing_on ? ring_slot(p) : 0;
+  record(p, slot, 0);
   rc = launch_pad_apodize(p, f, p->grid);
   if (rc) return rc;
-  record(p, 1);
+  record(p, slot, 1);
   rc = exec_fft(p, CUFFT_FORWARD);
   if (rc) return rc;
-  record(p, 2);
+  record(p, slot, 2);
   rc = p->prm.blocking ? launch_interp(p, p->grid, 0, fhat, 0) : launch_plain_interp(p, p->grid, 0, fhat, 0);
   if (rc) return rc;
-  record(p, 3);
-  if (p->timing_on) collect_timing(p, 0);
+  record(p, slot, 3);
+  finish_record(p, slot, 0);
   return NFFT_OK;
 }
 
 int nfft_adjoint(nfft_plan* p, const void* fhat, void* f) {
   int rc = require_nodes(p);
   if (rc) return rc;
-  record(p, 0);
+  const int slot = p->timing_on ? ring_slot(p) : 0;
+  record(p, slot, 0);
   rc = p->prm.blocking ? launch_spread(p, fhat, 0, p->grid, 0) : launch_plain_spread(p, fhat, 0, p->grid, 0);
   if (rc) return rc;
-  record(p, 1);
+  record(p, slot, 1);
   rc = exec_fft(p, CUFFT_INVERSE);
   if (rc) return rc;
-  record(p, 2);
+  record(p, slot, 2);
   rc = launch_crop_apodize(p, p->grid, f);
   if (rc) return rc;
-  record(p, 3);
-  if (p->timing_on) collect_timing(p, 1);
+  record(p, slot, 3);
+  finish_record(p, slot, 1);
   return NFFT_OK;
 }
 
@@ -720,7 +748,30 @@ void* nfft_grid(nfft_plan* p) { return p ? p->grid : nullptr; }
 int nfft_get_timing(nfft_plan* p, double out[7]) {
   if (!p || !out) return NFFT_ERR_INVALID_ARG;
   NFFT_CUDA_TRY(cudaStreamSynchronize(p->stream));
+  harvest_all(p);
   for (int i = 0; i < 7; ++i) out[i] = p->timing[i];
+  return NFFT_OK;
+}
+
+int nfft_get_timing_totals(nfft_plan* p, double totals[7], int64_t calls[2]) {
+  if (!p) return NFFT_ERR_INVALID_ARG;
+  NFFT_CUDA_TRY(cudaStreamSynchronize(p->stream));
+  harvest_all(p);
+  if (totals)
+    for (int i = 0; i < 7; ++i) totals[i] = p->timing_sum[i];
+  if (calls) {
+    calls[0] = p->timing_calls[0];
+    calls[1] = p->timing_calls[1];
+  }
+  return NFFT_OK;
+}
+
+int nfft_timing_reset(nfft_plan* p) {
+  if (!p) return NFFT_ERR_INVALID_ARG;
+  NFFT_CUDA_TRY(cudaStreamSynchronize(p->stream));
+  harvest_all(p);
+  for (int i = 1; i < 7; ++i) p->timing_sum[i] = 0.0;
+  p->timing_calls[0] = p->timing_calls[1] = 0;
   return NFFT_OK;
 }
 

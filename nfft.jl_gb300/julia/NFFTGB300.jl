@@ -1,0 +1,249 @@
+"""
+    NFFTGB300
+
+AbstractNFFTs backend whose plans run on one NVIDIA GB300 through the C ABI
+of `include/nfft_gb300.h` (libnfftgb300.so).  It is the drop-in replacement
+of NFFT.jl's GPU plan (ext/NFFTGPUArraysExt/implementation.jl): the same
+`plan_nfft(CuArray, k, N; m, σ, window, precompute, blocking)`, `mul!`,
+`adjoint`, `nodes!` and optional `convolve!`/`convolve_transpose!`/
+`deconvolve!`/`deconvolve_transpose!` surface, with the same exception types.
+
+Usage:
+    using CUDA, AbstractNFFTs, NFFTGB300
+    NFFTGB300.activate!()
+    p = plan_nfft(CuArray, k, N; m=4, σ=2.0)
+    fHat = p * CuArray(f)
+"""
+module NFFTGB300
+
+using AbstractNFFTs
+using LinearAlgebra
+using CUDA
+
+const libnfft = Ref{String}(joinpath(@__DIR__, "..", "nfftgb300", "libnfftgb300.so"))
+
+# ---------------------------------------------------------------- C structs
+
+struct CParams            # nfft_params
+  m::Int32
+  sigma::Float64
+  window::Int32
+  precompute::Int32
+  blocking::Int32
+  sort_nodes::Int32
+  store_deconv_idx::Int32
+  block_size::NTuple{3,Int64}
+  compensated::Int32
+  timing::Int32
+end
+
+struct CInfo              # nfft_info
+  precision::Int32
+  D::Int32
+  N::NTuple{3,Int64}
+  Ntilde::NTuple{3,Int64}
+  M::Int64
+  m::Int32
+  sigma::Float64
+  window::Int32
+  precompute::Int32
+  lut_size::Int64
+  block_size::NTuple{3,Int64}
+  num_tiles::Int64
+  num_spread_tasks::Int64
+  num_spread_entries::Int64
+  scratch_bytes::Int64
+end
+
+const WINDOWS = Dict(:kaiser_bessel => 0, :gauss => 1, :spline => 2, :kaiser_bessel_rev => 3, :cosh_type => 4)
+
+# Status codes -> the reference's exceptions (src/utils.jl:46-55, :98-105,
+# src/convolution.jl:47-53, src/windowFunctions.jl:16).
+function check(rc::Integer)
+  rc == 0 && return nothing
+  msg = unsafe_string(ccall((:nfft_last_error, libnfft[]), Cstring, ()))
+  (rc == 1 || rc == 3) && throw(ArgumentError(msg))
+  rc == 2 && throw(DimensionMismatch(msg))
+  rc == 8 && error(msg)
+  throw(ErrorException(unsafe_string(ccall((:nfft_status_string, libnfft[]), Cstring, (Cint,), rc)) * ": " * msg))
+end
+
+# ------------------------------------------------------------------ backend
+
+struct GB300Backend <: AbstractNFFTBackend end
+activate!() = AbstractNFFTs.set_active_backend!(NFFTGB300)
+backend() = GB300Backend()
+
+Base.@kwdef mutable struct GB300Params{T}
+  m::Int = 4
+  σ::T = 2.0
+  reltol::T = 1e-7
+  window::Symbol = :kaiser_bessel
+  LUTSize::Int = 0
+  precompute::AbstractNFFTs.PrecomputeFlags = AbstractNFFTs.POLYNOMIAL
+  sortNodes::Bool = false
+  storeDeconvolutionIdx::Bool = false
+  blocking::Bool = true
+  blockSize::NTuple{3,Int} = (0, 0, 0)
+end
+
+mutable struct GB300NFFTPlan{T,D} <: AbstractNFFTPlan{T,D,1}
+  handle::Ptr{Cvoid}
+  N::NTuple{D,Int}
+  NOut::NTuple{1,Int}
+  J::Int
+  k::Matrix{T}
+  Ñ::NTuple{D,Int}
+  dims::UnitRange{Int}
+  params::GB300Params{T}
+  tmpVec::CuArray{Complex{T},D}
+end
+
+function AbstractNFFTs.plan_nfft(::GB300Backend, ::Type{<:CuArray}, k::Matrix{T}, N::NTuple{D,Int}, rest...;
+                                 timing::Union{Nothing,TimingStats}=nothing, dims=1:D, fftflags=nothing,
+                                 window::Symbol=:kaiser_bessel, precompute=AbstractNFFTs.POLYNOMIAL,
+                                 blocking::Bool=true, sortNodes::Bool=false, storeDeconvolutionIdx::Bool=false,
+                                 blockSize=nothing, kwargs...) where {T<:Union{Float32,Float64},D}
+  dims != 1:D && error("GPU NFFT does not work along directions right now!")
+  size(k, 1) == D || throw(ArgumentError("Nodes x have dimension $(size(k,1)) != $D"))
+  haskey(WINDOWS, window) || error("Window $(window) not yet implemented!")
+  t = @elapsed begin
+    m, σ, reltol = AbstractNFFTs.accuracyParams(; kwargs...)
+    bs = blockSize === nothing ? (0, 0, 0) : ntuple(d -> d <= length(blockSize) ? blockSize[d] : 0, 3)
+    cp = CParams(m, σ, WINDOWS[window], Int(precompute), blocking, sortNodes, storeDeconvolutionIdx, bs, 0,
+                 timing === nothing ? 0 : 1)
+    Nc = Int64[N...; ones(Int64, 3 - D)]
+    h = Ref{Ptr{Cvoid}}(C_NULL)
+    check(ccall((:nfft_plan_create, libnfft[]), Cint,
+                (Ref{Ptr{Cvoid}}, Cint, Cint, Ptr{Int64}, Int64, Ref{CParams}, Ptr{Cvoid}),
+                h, T == Float32 ? 32 : 64, D, Nc, size(k, 2), cp, CUDA.stream().handle))
+    info = Ref{CInfo}()
+    check(ccall((:nfft_get_info, libnfft[]), Cint, (Ptr{Cvoid}, Ref{CInfo}), h[], info))
+    Ñ = ntuple(d -> Int(info[].Ntilde[d]), D)
+    grid = ccall((:nfft_grid, libnfft[]), Ptr{Cvoid}, (Ptr{Cvoid},), h[])
+    tmpVec = unsafe_wrap(CuArray, CuPtr{Complex{T}}(UInt(grid)), Ñ; own=false)
+    params = GB300Params{T}(; m, σ=T(info[].sigma), reltol=T(reltol), window, LUTSize=Int(info[].lut_size),
+                            precompute, sortNodes, storeDeconvolutionIdx, blocking,
+                            blockSize=ntuple(d -> Int(info[].block_size[d]), 3))
+    p = GB300NFFTPlan{T,D}(h[], N, (size(k, 2),), size(k, 2), k, Ñ, 1:D, params, tmpVec)
+    finalizer(p) do q
+      q.handle == C_NULL || ccall((:nfft_plan_destroy, libnfft[]), Cint, (Ptr{Cvoid},), q.handle)
+      q.handle = C_NULL
+    end
+    AbstractNFFTs.nodes!(p, k)
+  end
+  timing === nothing || (timing.pre = t)
+  return p
+end
+
+AbstractNFFTs.size_in(p::GB300NFFTPlan) = p.N
+AbstractNFFTs.size_out(p::GB300NFFTPlan) = p.NOut
+
+function bind_stream!(p::GB300NFFTPlan)
+  check(ccall((:nfft_set_stream, libnfft[]), Cint, (Ptr{Cvoid}, Ptr{Cvoid}), p.handle, CUDA.stream().handle))
+end
+
+function AbstractNFFTs.nodes!(p::GB300NFFTPlan{T}, k::Matrix{T}) where {T}
+  size(k, 2) == p.J || throw(DimensionMismatch("nodes! keeps the number of nodes; build a new plan for J ≠ $(p.J)"))
+  bind_stream!(p)
+  check(ccall((:nfft_set_nodes, libnfft[]), Cint, (Ptr{Cvoid}, Ptr{T}, Cint), p.handle, k, 0))
+  p.k = k
+  return p
+end
+
+function consistency(p::GB300NFFTPlan, f, fHat)
+  (size_in(p) == size(f) && size_out(p) == size(fHat)) ||
+    throw(DimensionMismatch("Data is not consistent with NFFTPlan"))
+end
+
+function LinearAlgebra.mul!(fHat::CuVector{Complex{T}}, p::GB300NFFTPlan{T,D}, f::CuArray{Complex{T},D};
+                            verbose=false, timing::Union{Nothing,TimingStats}=nothing) where {T,D}
+  consistency(p, f, fHat)
+  bind_stream!(p)
+  check(ccall((:nfft_forward, libnfft[]), Cint, (Ptr{Cvoid}, CuPtr{Complex{T}}, CuPtr{Complex{T}}),
+              p.handle, f, fHat))
+  timing === nothing || fill_timing!(p, timing)
+  return fHat
+end
+
+function LinearAlgebra.mul!(f::CuArray{Complex{T},D}, pl::Adjoint{Complex{T},<:GB300NFFTPlan{T,D}},
+                            fHat::CuVector{Complex{T}}; verbose=false,
+                            timing::Union{Nothing,TimingStats}=nothing) where {T,D}
+  p = pl.parent
+  consistency(p, f, fHat)
+  bind_stream!(p)
+  check(ccall((:nfft_adjoint, libnfft[]), Cint, (Ptr{Cvoid}, CuPtr{Complex{T}}, CuPtr{Complex{T}}),
+              p.handle, fHat, f))
+  timing === nothing || fill_timing!(p, timing)
+  return f
+end
+
+function fill_timing!(p::GB300NFFTPlan, t::TimingStats)
+  v = zeros(Float64, 7)
+  check(ccall((:nfft_get_timing, libnfft[]), Cint, (Ptr{Cvoid}, Ptr{Float64}), p.handle, v))
+  t.conv, t.fft, t.deconv = v[2], v[3], v[4]
+  t.conv_adjoint, t.fft_adjoint, t.deconv_adjoint = v[5], v[6], v[7]
+  return t
+end
+
+# Optional interface; real arrays are accepted for NFFTTools.sdc.
+const RC{T} = Union{T,Complex{T}}
+
+function AbstractNFFTs.convolve!(p::GB300NFFTPlan{T,D}, g::CuArray{<:RC{T},D}, fHat::CuVector{<:RC{T}}) where {T,D}
+  size(g) == p.Ñ || throw(DimensionMismatch("size(g)=$(size(g)) ≠ Ñ = $(p.Ñ)"))
+  size(fHat) == (p.J,) || throw(DimensionMismatch("size(fHat)=$(size(fHat)) ≠ J = $(p.J)"))
+  bind_stream!(p)
+  check(ccall((:nfft_convolve, libnfft[]), Cint, (Ptr{Cvoid}, CuPtr{Cvoid}, Cint, CuPtr{Cvoid}, Cint),
+              p.handle, g, eltype(g) <: Real, fHat, eltype(fHat) <: Real))
+  return fHat
+end
+
+function AbstractNFFTs.convolve_transpose!(p::GB300NFFTPlan{T,D}, fHat::CuVector{<:RC{T}},
+                                           g::CuArray{<:RC{T},D}) where {T,D}
+  size(g) == p.Ñ || throw(DimensionMismatch("size(g)=$(size(g)) ≠ Ñ = $(p.Ñ)"))
+  size(fHat) == (p.J,) || throw(DimensionMismatch("size(fHat)=$(size(fHat)) ≠ J = $(p.J)"))
+  bind_stream!(p)
+  check(ccall((:nfft_convolve_transpose, libnfft[]), Cint, (Ptr{Cvoid}, CuPtr{Cvoid}, Cint, CuPtr{Cvoid}, Cint),
+              p.handle, fHat, eltype(fHat) <: Real, g, eltype(g) <: Real))
+  return g
+end
+
+function AbstractNFFTs.deconvolve!(p::GB300NFFTPlan{T,D}, f::CuArray{Complex{T},D}, g::CuArray{Complex{T},D}) where {T,D}
+  bind_stream!(p)
+  check(ccall((:nfft_deconvolve, libnfft[]), Cint, (Ptr{Cvoid}, CuPtr{Complex{T}}, CuPtr{Complex{T}}),
+              p.handle, f, g))
+  return g
+end
+
+function AbstractNFFTs.deconvolve_transpose!(p::GB300NFFTPlan{T,D}, g::CuArray{Complex{T},D},
+                                             f::CuArray{Complex{T},D}) where {T,D}
+  bind_stream!(p)
+  check(ccall((:nfft_deconvolve_transpose, libnfft[]), Cint, (Ptr{Cvoid}, CuPtr{Complex{T}}, CuPtr{Complex{T}}),
+              p.handle, g, f))
+  return f
+end
+
+"""
+    grad_nodes!(dk, p, v, w)
+
+dk[d, j] = Re(conj(w[j]) * ∂(A v)_j / ∂k[d, j]); the node gradient the
+ChainRules pullback of `p * v` uses (no reference counterpart).
+"""
+function grad_nodes!(dk::CuMatrix{T}, p::GB300NFFTPlan{T,D}, v::CuArray{Complex{T},D},
+                     w::CuVector{Complex{T}}) where {T,D}
+  bind_stream!(p)
+  check(ccall((:nfft_grad_nodes, libnfft[]), Cint,
+              (Ptr{Cvoid}, CuPtr{Complex{T}}, CuPtr{Complex{T}}, CuPtr{T}), p.handle, v, w, dk))
+  return dk
+end
+
+function Base.copy(p::GB300NFFTPlan{T,D}) where {T,D}
+  AbstractNFFTs.plan_nfft(GB300Backend(), CuArray, copy(p.k), p.N; m=p.params.m, σ=p.params.σ,
+                          window=p.params.window, precompute=p.params.precompute, blocking=p.params.blocking)
+end
+
+Base.show(io::IO, p::GB300NFFTPlan) =
+  print(io, "GB300NFFTPlan with ", p.J, " sampling points for an input array of size", p.N,
+        " and an output array of size", p.NOut, " with dims ", p.dims)
+
+end # module

@@ -82,6 +82,8 @@ SIGNATURES = {
     "nfft_get_info": (_I, [_P, ctypes.POINTER(nfft_info)]),
     "nfft_grid": (_P, [_P]),
     "nfft_get_timing": (_I, [_P, ctypes.POINTER(ctypes.c_double)]),
+    "nfft_get_timing_totals": (_I, [_P, ctypes.POINTER(ctypes.c_double), _I64P]),
+    "nfft_timing_reset": (_I, [_P]),
     "nfft_get_binning": (_I, [_P, _I32P, _I32P, _I32P]),
     "nfft_get_deconv_factors": (_I, [_P, _P]),
     "nfft_sync": (_I, [_P]),

@@ -138,6 +138,8 @@ def as_colmajor(x, N, dtype, device="cuda"):
     """Move ``x`` (numpy or torch, logical shape N) to a column-major device
     tensor of ``dtype``; copies only when needed."""
     N = tuple(int(n) for n in N)
+    if tuple(x.shape) != N:
+        raise DimensionMismatch("Data is not consistent with NFFTPlan")
     if isinstance(x, np.ndarray):
         x = torch.from_numpy(np.ascontiguousarray(np.asarray(x).ravel(order="F")).reshape(N[::-1]))
         x = x.permute(*reversed(range(len(N))))
@@ -200,7 +202,10 @@ class GB300NFFTPlan:
         self.dtype = torch.float32 if kk.dtype in (np.float32, torch.float32) else torch.float64
         self.cdtype = torch.complex64 if self.dtype == torch.float32 else torch.complex128
         self.precision = 32 if self.dtype == torch.float32 else 64
-        self.device = torch.device(device)
+        dev = torch.device(device)
+        if dev.type == "cuda" and dev.index is None:
+            dev = torch.device("cuda", torch.cuda.current_device())
+        self.device = dev
         self.N = N
         self.dims = tuple(range(1, D + 1))
         self.params = NFFTParams(m=m_, sigma=s_, reltol=r_, window=window, precompute=PrecomputeFlags(precompute),

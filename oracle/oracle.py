@@ -422,3 +422,26 @@ def rel_l2(x, ref):
     x = np.asarray(x).ravel()
     ref = np.asarray(ref).ravel()
     return float(np.linalg.norm(x - ref) / np.linalg.norm(ref))
+
+
+def sdc(plan, iters=20):
+    """Sampling density compensation, restating NFFTTools sdc!
+    (NFFTTools/src/samplingDensity.jl:93-155) on an OraclePlan with the real
+    convolve / convolve_transpose of the optional interface."""
+    rdt = plan.dtype
+    weights = np.ones(plan.M, rdt)
+    scaling = None
+    for i in range(iters):
+        workg = np.real(plan.convolve_transpose(weights.astype(plan.cdtype))).astype(rdt)
+        if i == 0:
+            scaling = workg.max()
+        workg = workg / scaling
+        wt = np.real(plan.convolve(workg.astype(plan.cdtype))).astype(rdt) / scaling
+        if np.any(wt <= 0):
+            raise ValueError("non-positive weights")
+        weights = weights / wt
+    u = np.ones(plan.N, plan.cdtype)
+    workf = plan.forward(u) * weights
+    workv = plan.adjoint(workf)
+    c = np.real(workv.sum()) / np.sum(np.abs(workv) ** 2)
+    return (weights * c).astype(rdt)

@@ -1,0 +1,68 @@
+"""C-ABI library: it loads without a GPU and exports every entry point that
+include/nfft_gb300.h declares, with the binding's signatures.  No compute
+calls are made here."""
+import ctypes
+import os
+import re
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HEADER = os.path.join(ROOT, "include", "nfft_gb300.h")
+
+
+def declared_functions():
+    text = open(HEADER).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(nfft_[a-z_0-9]+)\s*\(", text)))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    import nfftgb300
+    if not os.path.exists(nfftgb300.LIB_PATH):
+        import __graft_entry__
+        __graft_entry__.build()
+    return nfftgb300.load()
+
+
+def test_library_exports_header(lib):
+    names = declared_functions()
+    assert len(names) >= 20
+    for n in names:
+        assert hasattr(lib, n), n
+
+
+def test_binding_covers_header():
+    import nfftgb300
+    assert set(declared_functions()) == set(nfftgb300.exported_symbols())
+
+
+def test_status_strings_and_defaults(lib):
+    import nfftgb300._lib as L
+    assert lib.nfft_status_string(0) == b"ok"
+    assert lib.nfft_status_string(L.NFFT_ERR_DIM_MISMATCH) == b"dimension mismatch"
+    prm = L.nfft_params()
+    lib.nfft_params_default(ctypes.byref(prm))
+    assert (prm.m, prm.sigma, prm.window, prm.precompute, prm.blocking) == (4, 2.0, 0, 4, 1)
+
+
+def test_plan_create_rejects_bad_arguments_without_gpu(lib):
+    """Argument validation happens before any device call."""
+    import nfftgb300._lib as L
+    prm = L.nfft_params()
+    lib.nfft_params_default(ctypes.byref(prm))
+    h = ctypes.c_void_p()
+    N = (ctypes.c_int64 * 3)(16, 16, 1)
+    assert lib.nfft_plan_create(ctypes.byref(h), 16, 2, N, 10, ctypes.byref(prm), None) == L.NFFT_ERR_INVALID_ARG
+    assert lib.nfft_plan_create(ctypes.byref(h), 32, 4, N, 10, ctypes.byref(prm), None) == L.NFFT_ERR_UNSUPPORTED
+    prm.m = 9
+    assert lib.nfft_plan_create(ctypes.byref(h), 32, 2, N, 10, ctypes.byref(prm), None) == L.NFFT_ERR_UNSUPPORTED
+    assert b"m = 9" in lib.nfft_last_error()
+    prm.m = 4
+    prm.window = 7
+    assert lib.nfft_plan_create(ctypes.byref(h), 32, 2, N, 10, ctypes.byref(prm), None) == L.NFFT_ERR_UNSUPPORTED
+    prm.window = 0
+    prm.precompute = 0
+    assert lib.nfft_plan_create(ctypes.byref(h), 32, 2, N, 10, ctypes.byref(prm), None) == L.NFFT_ERR_UNSUPPORTED
+    assert not h.value

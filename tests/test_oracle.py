@@ -1,0 +1,157 @@
+"""The oracle (CPU restatement of NFFT.jl) pinned against the reference's own
+known-answer tests and published accuracy, and against the golden fixtures."""
+import os
+
+import numpy as np
+import pytest
+
+from oracle import oracle
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+# test/accuracy.jl:46 -- window -> tolerance at m=5, sigma=2
+TABLE = [("kaiser_bessel", 1e-7), ("cosh_type", 1e-7), ("gauss", 1e-3), ("kaiser_bessel_rev", 1e-6),
+         ("spline", 1e-4)]
+
+
+@pytest.mark.parametrize("N", [(255,), (31, 33), (11, 12, 14)])
+@pytest.mark.parametrize("window,eps", TABLE)
+@pytest.mark.parametrize("pre", [oracle.TENSOR, oracle.LINEAR, oracle.FULL])
+def test_accuracy_table(N, window, eps, pre):
+    """test/accuracy.jl:41-73 (J = |N|, random nodes, NDFT ground truth)."""
+    rng = np.random.default_rng(123)
+    D = len(N)
+    J = int(np.prod(N))
+    k = rng.random((D, J)) - 0.5
+    fhat = rng.random(J) + 1j * rng.random(J)
+    p = oracle.OraclePlan(k, N, m=5, sigma=2.0, window=window, precompute=pre)
+    f = oracle.ndft_adjoint(k, N, fhat)
+    assert oracle.rel_l2(p.adjoint(fhat), f) < eps
+    g = oracle.ndft_forward(k, f)
+    assert oracle.rel_l2(p.forward(f), g) < eps
+
+
+def test_high_level_fp32():
+    """test/accuracy.jl:6-39: Float32 data, N = (33, 35), tolerance 1e-3."""
+    rng = np.random.default_rng(1)
+    N = (33, 35)
+    J = int(np.prod(N))
+    k = rng.random((2, J)) - 0.5
+    fhat = rng.random(J) + 1j * rng.random(J)
+    p = oracle.OraclePlan(k.astype(np.float32), N, reltol=1e-9, dtype=np.float32)
+    f = oracle.ndft_adjoint(k.astype(np.float32), N, fhat.astype(np.complex64))
+    assert oracle.rel_l2(p.adjoint(fhat.astype(np.complex64)), f) < 1e-3
+
+
+@pytest.mark.parametrize("m,published", [(3, 7.66e-6), (4, 5.75e-8), (5, 6.13e-10), (6, 8.92e-12)])
+def test_paper_accuracy_band(m, published):
+    """benchmark/paper/img/accuracy_m_D2_.tex:36 -- TENSOR forward rel l2 error
+    at D=2, sigma=2 (published for N=512^2); a 2-D 96^2 case must land within
+    a factor 3 of the published value."""
+    rng = np.random.default_rng(11)
+    N = (96, 96)
+    J = int(np.prod(N))
+    k = rng.random((2, J)) - 0.5
+    f = rng.random(N) + 1j * rng.random(N)
+    sub = rng.choice(J, 400, replace=False)
+    g = oracle.ndft_forward(k, f, subset=sub)
+    p = oracle.OraclePlan(k, N, m=m, sigma=2.0, precompute=oracle.TENSOR)
+    e = oracle.rel_l2(p.forward(f)[sub], g)
+    assert published / 3 < e < published * 3
+
+
+@pytest.mark.parametrize("pre", [oracle.LINEAR, oracle.FULL, oracle.TENSOR, oracle.POLYNOMIAL])
+def test_sdc_equispaced(pre):
+    """test/samplingDensity.jl:10-27: 9x8 equispaced nodes give weights 1/72."""
+    N = (9, 8)
+    xs = (np.arange(N[0]) / N[0] - 0.5).astype(np.float32)
+    ys = (np.arange(N[1]) / N[1] - 0.5).astype(np.float32)
+    nodes = np.array([[x, y] for y in ys for x in xs], dtype=np.float32).T
+    p = oracle.OraclePlan(nodes, N, m=5, sigma=2.0, precompute=pre, dtype=np.float32)
+    w = oracle.sdc(p, iters=10)
+    assert w.dtype == np.float32
+    assert np.all(w > 0)
+    np.testing.assert_allclose(w, 1 / 72, rtol=np.sqrt(np.finfo(np.float32).eps))
+
+
+def test_issue_106_node():
+    """test/issues.jl:3-17: node 0.008333333 with N = 240, LINEAR, no throw."""
+    trj = np.full((1, 2), 0.008333333, np.float32)
+    p = oracle.OraclePlan(trj, (240,), precompute=oracle.LINEAR, dtype=np.float32)
+    out = p.adjoint(np.ones(2, np.complex64))
+    assert np.all(np.isfinite(out))
+
+
+def test_node_checks():
+    with pytest.raises(ValueError):
+        oracle.OraclePlan(np.array([[-0.6, 0.9], [0.5, -0.5]]), (2, 2))
+    with pytest.raises(ValueError):
+        oracle.OraclePlan(np.array([[-0.3, 0.3], [0.3, np.nan]]), (2, 2))
+    with pytest.raises(ValueError):
+        oracle.OraclePlan(np.zeros((1, 4)), (2, 2))
+
+
+def test_params():
+    """initParams / accuracyParams (src/precomputation.jl:3-56, misc.jl:44-81)."""
+    assert oracle.accuracy_params() == (5, 2.0, 1e-9)
+    assert oracle.accuracy_params(reltol=1e-7)[:2] == (4, 2.0)
+    assert oracle.accuracy_params(m=3)[:2] == (5, 2.0)  # m alone is ignored
+    assert oracle.accuracy_params(m=3, sigma=1.5)[:2] == (3, 1.5)
+    assert oracle.oversampled((11, 255), 1.5) == (16, 382)
+    assert oracle.lut_size(4) == 2 ** 14 * 4
+    assert oracle.default_block_size((512, 512, 512)) == (16, 16, 16)
+    assert oracle.default_block_size((256, 256)) == (64, 64)
+    assert oracle.default_block_size((100,)) == (100,)
+
+
+def test_chebyshev_deconv_close_to_exact():
+    """The 30-point Chebyshev interpolant of phi-hat (src/precomputation.jl:351)
+    differs from the exact 1/phi-hat by far less than the 1e-11 FP64 budget."""
+    for N in [(64,), (256,), (31,)]:
+        Nt = oracle.oversampled(N, 2.0)
+        a = oracle.deconv_factors("kaiser_bessel", N, Nt, 4, 2.0)[0]
+        b = oracle.deconv_factors("kaiser_bessel", N, Nt, 4, 2.0, exact=True)[0]
+        assert np.max(np.abs(a - b) / np.abs(b)) < 1e-13
+
+
+def test_blocking_stable_against_numpy():
+    """Block ids and the stable in-block order (src/precomputation.jl:487-520)
+    against an independent numpy restatement (stable argsort)."""
+    rng = np.random.default_rng(3)
+    for dtype in (np.float64, np.float32):
+        k = (rng.random((3, 5000)) - 0.5).astype(dtype)
+        p = oracle.OraclePlan(k, (20, 24, 18), m=4, sigma=2.0, dtype=dtype)
+        b = p.blocks()
+        ks = k.copy()
+        ks[ks < 0] += dtype(1)
+        ks[ks == 1] -= np.finfo(dtype).eps
+        kscale = ks * np.array(p.Nt, dtype)[:, None]
+        t = np.minimum(np.trunc(kscale).astype(np.int64), np.array(p.Nt)[:, None] - 1)
+        bi = t // np.array(p.block_size)[:, None]
+        nb = [-(-n // s) for n, s in zip(p.Nt, p.block_size)]
+        lin = bi[0] + nb[0] * (bi[1] + nb[1] * bi[2])
+        assert np.array_equal(b["trunc"], t)
+        assert np.array_equal(b["bins"], lin)
+        assert np.array_equal(b["nodes"], np.argsort(lin, kind="stable"))
+
+
+@pytest.mark.parametrize("name", ["d1", "d2", "d3"])
+def test_golden(name):
+    z = np.load(os.path.join(GOLDEN, f"{name}.npz"))
+    k, f, fhat, N = z["k"], z["f"], z["fhat"], tuple(z["N"])
+    np.testing.assert_allclose(oracle.ndft_forward(k, f), z["ndft_forward"], rtol=1e-12, atol=1e-12)
+    np.testing.assert_allclose(oracle.ndft_adjoint(k, N, fhat), z["ndft_adjoint"], rtol=1e-12, atol=1e-12)
+    # direct check of the NDFT definition (src/direct.jl:99-123) with numpy
+    grids = np.meshgrid(*[np.arange(n) - n // 2 for n in N], indexing="ij")
+    ph = sum(k[d][:, None] * grids[d].ravel(order="F")[None, :] for d in range(len(N)))
+    direct = np.exp(-2j * np.pi * ph) @ f.ravel(order="F")
+    np.testing.assert_allclose(direct, z["ndft_forward"], rtol=1e-10, atol=1e-10)
+    op = oracle.OraclePlan(k, N, m=4, sigma=2.0, precompute=oracle.TENSOR)
+    assert oracle.rel_l2(op.forward(f), z["nfft_forward_m4"]) < 1e-13
+    assert oracle.rel_l2(op.adjoint(fhat), z["nfft_adjoint_m4"]) < 1e-13
+    assert oracle.rel_l2(z["nfft_forward_m4"], z["ndft_forward"]) < 1e-6
+    assert oracle.rel_l2(z["nfft_adjoint_m4"], z["ndft_adjoint"]) < 1e-6
+    b = op.blocks()
+    assert np.array_equal(b["block_start"], z["block_start"])
+    assert np.array_equal(b["nodes"], z["block_nodes"])
+    assert np.array_equal(b["trunc"], z["trunc"])
