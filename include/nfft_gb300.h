@@ -208,6 +208,25 @@ int nfft_get_binning(nfft_plan* plan, int32_t* perm, int32_t* tile_start, int32_
  * values of the plan's real type. */
 int nfft_get_deconv_factors(nfft_plan* plan, void* out);
 
+/* Node binning without any device allocation.  No counterpart in the
+ * reference: it is the binning step of nfft_set_nodes (node check, reduction
+ * to grid index, stable radix sort by tile -- the nodesInBlock order of
+ * src/precomputation.jl:487-520) for callers that cannot call cudaMalloc at
+ * that point, e.g. a host framework whose caching allocator already owns the
+ * device memory, or a latency-critical pipeline that must not take the
+ * implicit device synchronisation of cudaMalloc/cudaFree.  The caller passes
+ * the nodes k (device, D x M of the real type), perm (device, M int32: node
+ * at sorted position i) and tile_start (device, num_tiles+1 int32 CSR
+ * offsets), with num_tiles = prod_d ceil(Ntilde[d] / block_size[d]).
+ * Scratch is a static 16 MiB device array that every GPU loading the
+ * library holds until exit; the limits are M <= 262144 nodes and
+ * num_tiles <= 262144, larger requests fail with NFFT_ERR_UNSUPPORTED.  The
+ * first call on a device looks up the array's device address (make it before
+ * any stream capture).  All calls share the array: calls that overlap on the
+ * GPU race.  Synchronises the stream once (node check). */
+int nfft_bin_nodes_noalloc(int precision, int D, const int64_t* Ntilde, const int64_t* block_size, int64_t M,
+                           const void* k, int32_t* perm, int32_t* tile_start, void* stream);
+
 /* Wait for the plan's stream. */
 int nfft_sync(nfft_plan* plan);
 
