@@ -99,15 +99,14 @@ __global__ void __launch_bounds__(kGradThreads) grad_nodes_kernel(Geom<T> G, Nod
     T W0 = 0, W1 = 0, V0 = 0, V1 = 0;  // weights and derivatives
     if (lane < D * L) {
       const int d = lane / L;
-      tap_weight_deriv<T>(G, cs, Nd.te[int64_t(d) * Nd.M + i], lane - d * L, W0, V0);
+      tap_weight_deriv<T>(G, cs, Nd.frac4[4 * i + d], lane - d * L, W0, V0);
     }
     if (D * L > 32 && lane + 32 < D * L) {
       const int q = lane + 32, d = q / L;
-      tap_weight_deriv<T>(G, cs, Nd.te[int64_t(d) * Nd.M + i], q - d * L, W1, V1);
+      tap_weight_deriv<T>(G, cs, Nd.frac4[4 * i + d], q - d * L, W1, V1);
     }
-    int t[3] = {0, 0, 0};
-#pragma unroll
-    for (int d = 0; d < D; ++d) t[d] = Nd.ti[int64_t(d) * Nd.M + i];
+    const int4 nd = Nd.node4[i];
+    const int t[3] = {nd.x, nd.y, nd.z};
     const int gx = G.small_grid ? wrap_any(t[0] - m + 1 + ix, G.Nt[0]) : wrap_once(t[0] - m + 1 + ix, G.Nt[0]);
     const T wx = wsel<L, D>(W0, W1, ix), dwx = wsel<L, D>(V0, V1, ix);
     T sr[D], si[D];
@@ -159,7 +158,7 @@ __global__ void __launch_bounds__(kGradThreads) grad_nodes_kernel(Geom<T> G, Nod
       }
     }
     if (lane == 0) {
-      const int64_t j = Nd.perm[i];
+      const int64_t j = nd.w;
       const C w = wv[j];
 #pragma unroll
       for (int d = 0; d < D; ++d) {

@@ -66,10 +66,15 @@ template <typename T> struct Geom {
 };
 
 // Sorted node data produced by nfft_set_nodes.
+//   node4[i] = {trunc_x, trunc_y, trunc_z, input index j} of the node at sorted
+//              position i (trunc = trunc(k_shift * Ntilde), 0 in singleton dims);
+//   frac4[4i + d] = fractional offset e_d in [0,1) (a hair outside for FP32);
+//   wtab[i*D*2m + d*2m + l] = window value of tap l in dimension d (the window
+//              tensor; stored unless the precompute mode is POLYNOMIAL).
 template <typename T> struct Nodes {
-  const int32_t* perm;    // sorted position -> node id
-  const int32_t* ti;      // D x M (SoA, dim-major): trunc(k_shift * Ntilde), sorted order
-  const T* te;            // D x M (SoA): fractional offset e in [0,1) (slightly outside for FP32)
+  const int4* node4;
+  const T* frac4;
+  const T* wtab;
   int64_t M;
 };
 
@@ -101,18 +106,15 @@ struct nfft_plan {
 
   bool has_nodes = false;
   void* k = nullptr;          // D x M nodes (T), user order
-  int32_t* perm = nullptr;    // M
-  int32_t* ti = nullptr;      // D x M sorted
-  void* te = nullptr;         // D x M sorted (T)
-  int32_t* tile_start = nullptr;   // ntiles_total + 1 (nodes per home tile)
+  int4* node4 = nullptr;      // M, sorted: trunc per dim + input index
+  void* frac4 = nullptr;      // 4M (T), sorted: fractional offsets
+  void* wtab = nullptr;       // M * D * 2m (T), sorted window tensor (not for POLYNOMIAL)
+  int32_t* tile_start = nullptr;   // ntiles_total + 1: CSR of nodes per home tile
   void* cbuf = nullptr;       // M complex scratch for real-valued convolve calls (lazy)
-  // spreading task list (owner-computes tiles)
-  int64_t n_entries = 0;
-  int32_t* entries = nullptr;      // sorted node ids grouped by tile
+  // spreading tasks: (home tile, first node, end node, 0), hot tiles split
   int64_t n_tasks = 0;
-  int4* tasks = nullptr;           // (tile, begin, end, multi)
-  int64_t n_multi = 0;
-  int32_t* multi_tiles = nullptr;  // tiles written by more than one task
+  int4* tasks = nullptr;
+  int spread_pitch = 0;            // shared-memory row pitch of the padded tile
   int* dflag = nullptr;            // device status word
   size_t scratch_bytes = 0;
 
@@ -136,12 +138,10 @@ namespace nfft {
 int launch_check_nodes(const nfft_plan* p, const void* k, int* flag);
 int launch_reduce_nodes(const nfft_plan* p, const void* k, int32_t* ti_u, void* te_u, uint32_t* key,
                         int32_t* val, int32_t* tile_count);
-int launch_gather_sorted(const nfft_plan* p, const int32_t* perm, const int32_t* ti_u, const void* te_u);
+int launch_build_node_tables(const nfft_plan* p, const int32_t* perm, const int32_t* ti_u, const void* te_u);
+int launch_build_weight_table(const nfft_plan* p);
 int launch_deconv_factors(nfft_plan* p);
-int launch_count_entries(const nfft_plan* p, int32_t* ecount);
-int launch_fill_entries(const nfft_plan* p, const int32_t* eoff, uint32_t* ekey, int32_t* eval,
-                        int32_t* tcount);
-int launch_build_tasks(nfft_plan* p, const int32_t* tile_estart, int chunk);
+int launch_build_tasks(nfft_plan* p, int chunk);
 // sort.cu
 int radix_sort_pairs(uint32_t* keys, int32_t* vals, uint32_t* keys_tmp, int32_t* vals_tmp, int64_t n,
                      int key_bits, void* scratch, size_t scratch_bytes, cudaStream_t s,

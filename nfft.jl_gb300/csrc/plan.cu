@@ -6,6 +6,7 @@
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
+#include <algorithm>
 #include <cstring>
 #include <vector>
 
@@ -50,12 +51,14 @@ template Geom<double> make_geom<double>(const nfft_plan*);
 
 template <typename T> Nodes<T> make_nodes(const nfft_plan* p) {
   Nodes<T> n{};
-  n.perm = p->perm;
-  n.ti = p->ti;
-  n.te = static_cast<const T*>(p->te);
+  n.node4 = p->node4;
+  n.frac4 = static_cast<const T*>(p->frac4);
+  n.wtab = static_cast<const T*>(p->wtab);
   n.M = p->M;
   return n;
 }
+
+int spread_pitch_for(int D, int m, int P0, int elem_bytes);
 template Nodes<float> make_nodes<float>(const nfft_plan*);
 template Nodes<double> make_nodes<double>(const nfft_plan*);
 
@@ -143,17 +146,16 @@ void default_block(nfft_plan* p) {
 
 void free_nodes(nfft_plan* p) {
   cudaFree(p->k);
-  cudaFree(p->perm);
-  cudaFree(p->ti);
-  cudaFree(p->te);
+  cudaFree(p->node4);
+  cudaFree(p->frac4);
+  cudaFree(p->wtab);
   cudaFree(p->tile_start);
-  cudaFree(p->entries);
   cudaFree(p->tasks);
-  cudaFree(p->multi_tiles);
-  p->k = p->te = nullptr;
-  p->perm = p->ti = p->tile_start = p->entries = p->multi_tiles = nullptr;
+  p->k = p->frac4 = p->wtab = nullptr;
+  p->node4 = nullptr;
+  p->tile_start = nullptr;
   p->tasks = nullptr;
-  p->n_entries = p->n_tasks = p->n_multi = 0;
+  p->n_tasks = 0;
   p->has_nodes = false;
 }
 
@@ -339,6 +341,11 @@ int nfft_plan_create(nfft_plan** out, int precision, int D, const int64_t* N, in
     }
     total *= p->Nt[d];
   }
+  if (D >= 2 && p->Nt[0] * p->Nt[1] >= (int64_t(1) << 31)) {
+    delete p;
+    set_error("oversampled planes of 2^31 or more points are not supported");
+    return NFFT_ERR_UNSUPPORTED;
+  }
   if (total >= (int64_t(1) << 34)) {
     delete p;
     set_error("oversampled grid of %lld points too large", (long long)total);
@@ -347,6 +354,7 @@ int nfft_plan_create(nfft_plan** out, int precision, int D, const int64_t* N, in
   p->sigma = double(p->Nt[0]) / double(p->N[0]);  // sigma = Ntilde/N, :30
   p->lut_size = lut_size_for(p->m);
   default_block(p);
+  p->spread_pitch = spread_pitch_for(D, p->m, int(p->bs[0]) + 2 * p->m - 1, precision == 32 ? 4 : 8);
   p->ntiles_total = 1;
   for (int d = 0; d < 3; ++d) {
     p->ntiles[d] = (p->Nt[d] + p->bs[d] - 1) / p->bs[d];
@@ -470,10 +478,12 @@ int nfft_set_nodes(nfft_plan* p, const void* k, int k_on_device) {
   const int64_t M = p->M, D = p->D;
   const size_t rs = p->real_size;
   cudaStream_t s = p->stream;
+  const int L = 2 * p->m;
+  const bool table = p->prm.precompute != NFFT_PRECOMPUTE_POLYNOMIAL;
   if (cudaMalloc(&p->k, rs * size_t(D * M > 0 ? D * M : 1)) != cudaSuccess ||
-      cudaMalloc(&p->perm, sizeof(int32_t) * size_t(M > 0 ? M : 1)) != cudaSuccess ||
-      cudaMalloc(&p->ti, sizeof(int32_t) * size_t(D * M > 0 ? D * M : 1)) != cudaSuccess ||
-      cudaMalloc(&p->te, rs * size_t(D * M > 0 ? D * M : 1)) != cudaSuccess ||
+      cudaMalloc(&p->node4, sizeof(int4) * size_t(M > 0 ? M : 1)) != cudaSuccess ||
+      cudaMalloc(&p->frac4, rs * 4 * size_t(M > 0 ? M : 1)) != cudaSuccess ||
+      (table && cudaMalloc(&p->wtab, rs * size_t(M > 0 ? M * D * L : 1)) != cudaSuccess) ||
       cudaMalloc(&p->tile_start, sizeof(int32_t) * size_t(p->ntiles_total + 1)) != cudaSuccess) {
     free_nodes(p);
     set_error("cudaMalloc of node arrays failed");
@@ -518,64 +528,24 @@ int nfft_set_nodes(nfft_plan* p, const void* k, int k_on_device) {
     rc = radix_sort_pairs(static_cast<uint32_t*>(key.p), static_cast<int32_t*>(val.p), static_cast<uint32_t*>(key2.p),
                           static_cast<int32_t*>(val2.p), M, kbits, scr.p, sb, s, &ko, &vo);
     if (rc) return rc;
-    if (M > 0) NFFT_CUDA_TRY(cudaMemcpyAsync(p->perm, vo, sizeof(int32_t) * size_t(M), cudaMemcpyDeviceToDevice, s));
     rc = exclusive_scan_i32(static_cast<int32_t*>(tcount.p), p->tile_start, nt + 1, scr.p, sb, s);
     if (rc) return rc;
-    rc = launch_gather_sorted(p, p->perm, static_cast<int32_t*>(ti_u.p), te_u.p);
+    rc = launch_build_node_tables(p, vo, static_cast<int32_t*>(ti_u.p), te_u.p);
     if (rc) return rc;
     NFFT_CUDA_TRY(cudaStreamSynchronize(s));
   }
-  p->scratch_bytes = size_t(2) * rs * size_t(p->Nt[0] * p->Nt[1] * p->Nt[2]) + rs * size_t(D * M) * 2 +
-                     sizeof(int32_t) * size_t(M + D * M + nt + 1);
+  if (table) {
+    rc = launch_build_weight_table(p);
+    if (rc) return rc;
+  }
+  p->scratch_bytes = size_t(2) * rs * size_t(p->Nt[0] * p->Nt[1] * p->Nt[2]) + rs * size_t(D * M) +
+                     sizeof(int4) * size_t(M) + rs * 4 * size_t(M) + (table ? rs * size_t(M * D * L) : 0) +
+                     sizeof(int32_t) * size_t(nt + 1);
   if (p->prm.blocking) {
-    // spreading entries: (tile, sorted node) pairs for every tile a window touches
-    DevBuf ecount, eoff, scr;
-    NFFT_ALLOC(ecount, sizeof(int32_t) * size_t(M + 1));
-    NFFT_ALLOC(eoff, sizeof(int32_t) * size_t(M + 1));
-    const size_t sb1 = scan_scratch_bytes(std::max<int64_t>(M + 1, nt + 1));
-    NFFT_ALLOC(scr, sb1);
-    NFFT_CUDA_TRY(cudaMemsetAsync(ecount.p, 0, sizeof(int32_t) * size_t(M + 1), s));
-    rc = launch_count_entries(p, static_cast<int32_t*>(ecount.p));
+    // hot tiles are split into chunks of at most 1024 nodes
+    rc = launch_build_tasks(p, 1024);
     if (rc) return rc;
-    rc = exclusive_scan_i32(static_cast<int32_t*>(ecount.p), static_cast<int32_t*>(eoff.p), M + 1, scr.p, sb1, s);
-    if (rc) return rc;
-    int32_t E = 0;
-    NFFT_CUDA_TRY(cudaMemcpyAsync(&E, static_cast<int32_t*>(eoff.p) + M, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
-    NFFT_CUDA_TRY(cudaStreamSynchronize(s));
-    if (E < 0) {
-      set_error("too many spreading entries");
-      return NFFT_ERR_UNSUPPORTED;
-    }
-    DevBuf ekey, eval, ekey2, eval2, tcount, tstart, scr2;
-    NFFT_ALLOC(ekey, sizeof(uint32_t) * size_t(E));
-    NFFT_ALLOC(eval, sizeof(int32_t) * size_t(E));
-    NFFT_ALLOC(ekey2, sizeof(uint32_t) * size_t(E));
-    NFFT_ALLOC(eval2, sizeof(int32_t) * size_t(E));
-    NFFT_ALLOC(tcount, sizeof(int32_t) * size_t(nt + 1));
-    NFFT_ALLOC(tstart, sizeof(int32_t) * size_t(nt + 1));
-    const size_t sb2 = std::max(radix_sort_scratch_bytes(E), scan_scratch_bytes(nt + 1));
-    NFFT_ALLOC(scr2, sb2);
-    NFFT_CUDA_TRY(cudaMemsetAsync(tcount.p, 0, sizeof(int32_t) * size_t(nt + 1), s));
-    rc = launch_fill_entries(p, static_cast<int32_t*>(eoff.p), static_cast<uint32_t*>(ekey.p),
-                             static_cast<int32_t*>(eval.p), static_cast<int32_t*>(tcount.p));
-    if (rc) return rc;
-    uint32_t* ko = nullptr;
-    int32_t* vo = nullptr;
-    rc = radix_sort_pairs(static_cast<uint32_t*>(ekey.p), static_cast<int32_t*>(eval.p),
-                          static_cast<uint32_t*>(ekey2.p), static_cast<int32_t*>(eval2.p), E, kbits, scr2.p, sb2, s,
-                          &ko, &vo);
-    if (rc) return rc;
-    if (cudaMalloc(&p->entries, sizeof(int32_t) * size_t(E > 0 ? E : 1)) != cudaSuccess) {
-      set_error("cudaMalloc of spreading entries failed");
-      return NFFT_ERR_ALLOC;
-    }
-    if (E > 0) NFFT_CUDA_TRY(cudaMemcpyAsync(p->entries, vo, sizeof(int32_t) * size_t(E), cudaMemcpyDeviceToDevice, s));
-    p->n_entries = E;
-    rc = exclusive_scan_i32(static_cast<int32_t*>(tcount.p), static_cast<int32_t*>(tstart.p), nt + 1, scr2.p, sb2, s);
-    if (rc) return rc;
-    rc = launch_build_tasks(p, static_cast<int32_t*>(tstart.p), 2048);
-    if (rc) return rc;
-    p->scratch_bytes += sizeof(int32_t) * size_t(E);
+    p->scratch_bytes += sizeof(int4) * size_t(p->n_tasks);
   }
   NFFT_CUDA_TRY(cudaStreamSynchronize(s));
   NFFT_CUDA_TRY(cudaGetLastError());
@@ -738,7 +708,7 @@ int nfft_get_info(const nfft_plan* p, nfft_info* info) {
   info->lut_size = p->lut_size;
   info->num_tiles = p->ntiles_total;
   info->num_spread_tasks = p->n_tasks;
-  info->num_spread_entries = p->n_entries;
+  info->num_spread_entries = p->has_nodes ? p->M : 0;
   info->scratch_bytes = int64_t(p->scratch_bytes);
   return NFFT_OK;
 }
@@ -780,18 +750,18 @@ int nfft_get_binning(nfft_plan* p, int32_t* perm, int32_t* tile_start, int32_t* 
   if (rc) return rc;
   const int64_t M = p->M, D = p->D;
   NFFT_CUDA_TRY(cudaStreamSynchronize(p->stream));
-  std::vector<int32_t> hperm(M), hti(D * M);
-  if (M > 0) {
-    NFFT_CUDA_TRY(cudaMemcpy(hperm.data(), p->perm, sizeof(int32_t) * M, cudaMemcpyDeviceToHost));
-    NFFT_CUDA_TRY(cudaMemcpy(hti.data(), p->ti, sizeof(int32_t) * D * M, cudaMemcpyDeviceToHost));
-  }
-  if (perm && M > 0) std::memcpy(perm, hperm.data(), sizeof(int32_t) * M);
+  std::vector<int4> nodes(M > 0 ? M : 1);
+  if (M > 0) NFFT_CUDA_TRY(cudaMemcpy(nodes.data(), p->node4, sizeof(int4) * M, cudaMemcpyDeviceToHost));
+  if (perm)
+    for (int64_t i = 0; i < M; ++i) perm[i] = nodes[i].w;
   if (tile_start)
     NFFT_CUDA_TRY(cudaMemcpy(tile_start, p->tile_start, sizeof(int32_t) * (p->ntiles_total + 1), cudaMemcpyDeviceToHost));
   if (grid_index) {
-    for (int64_t i = 0; i < M; ++i)
+    for (int64_t i = 0; i < M; ++i) {
+      const int t[3] = {nodes[i].x, nodes[i].y, nodes[i].z};
       for (int d = 0; d < D; ++d)
-        grid_index[d + D * int64_t(hperm[i])] = int32_t(wrap_any(hti[d * M + i] - p->m + 1, int(p->Nt[d])));
+        grid_index[d + D * int64_t(nodes[i].w)] = int32_t(wrap_any(t[d] - p->m + 1, int(p->Nt[d])));
+    }
   }
   return NFFT_OK;
 }

@@ -42,15 +42,35 @@ __global__ void reduce_nodes_kernel(const T* __restrict__ k, int D, int64_t M, i
 }
 
 template <typename T>
-__global__ void gather_sorted_kernel(const int32_t* __restrict__ perm, int D, int64_t M,
-                                     const int32_t* __restrict__ ti_u, const T* __restrict__ te_u,
-                                     int32_t* __restrict__ ti, T* __restrict__ te) {
+__global__ void build_node_tables_kernel(const int32_t* __restrict__ perm, int D, int64_t M,
+                                         const int32_t* __restrict__ ti_u, const T* __restrict__ te_u,
+                                         int4* __restrict__ node4, T* __restrict__ frac4) {
   int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   if (i >= M) return;
   const int64_t j = perm[i];
+  int t[3] = {0, 0, 0};
+  T e[4] = {T(0), T(0), T(0), T(0)};
   for (int d = 0; d < D; ++d) {
-    ti[int64_t(d) * M + i] = ti_u[int64_t(d) * M + j];
-    te[int64_t(d) * M + i] = te_u[int64_t(d) * M + j];
+    t[d] = ti_u[int64_t(d) * M + j];
+    e[d] = te_u[int64_t(d) * M + j];
+  }
+  node4[i] = make_int4(t[0], t[1], t[2], int(j));
+  for (int d = 0; d < 4; ++d) frac4[4 * i + d] = e[d];
+}
+
+// Window tensor (src/precomputation.jl:556-591 for TENSOR; the window function
+// itself for FULL; the LUT for LINEAR): one thread per (node, dimension, tap).
+template <typename T>
+__global__ void build_weight_table_kernel(Geom<T> G, const T* __restrict__ frac4, int64_t M, T* __restrict__ wtab) {
+  const int L = 2 * G.m;
+  const int DL = G.D * L;
+  const int64_t total = M * DL;
+  for (int64_t q = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; q < total; q += int64_t(gridDim.x) * blockDim.x) {
+    const int64_t i = q / DL;
+    const int r = int(q - i * DL);
+    const int d = r / L;
+    const int l = r - d * L;
+    wtab[q] = tap_weight<T>(G, G.coeffs, frac4[4 * i + d], l);
   }
 }
 
@@ -165,82 +185,23 @@ __global__ void deconv_factors_kernel(int window, int m, double sigma, int D, in
   }
 }
 
-// ------------------------------------------------------- spreading entries
-// Distinct tiles touched, in one dimension, by the taps t-m+1 .. t+m of a
-// node (wrapped).  Returns the count; ids in out[].
-__device__ __forceinline__ int tiles_touched(int t, int m, int Nt, int bs, int* out) {
-  int n = 0;
-  const int L = 2 * m;
-  for (int l = 0; l < L; ++l) {
-    int g = wrap_any(t - m + 1 + l, Nt);
-    int tile = g / bs;
-    bool seen = false;
-    for (int q = 0; q < n; ++q) seen |= (out[q] == tile);
-    if (!seen) out[n++] = tile;
-  }
-  return n;
-}
-
-__global__ void count_entries_kernel(const int32_t* __restrict__ ti, int D, int64_t M, int m, int Nt0, int Nt1,
-                                     int Nt2, int bs0, int bs1, int bs2, int32_t* __restrict__ ecount) {
-  int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (i >= M) return;
-  const int Nt[3] = {Nt0, Nt1, Nt2};
-  const int bs[3] = {bs0, bs1, bs2};
-  int tl[kMaxL];
-  int c = 1;
-  for (int d = 0; d < D; ++d) c *= tiles_touched(ti[int64_t(d) * M + i], m, Nt[d], bs[d], tl);
-  ecount[i] = c;
-}
-
-__global__ void fill_entries_kernel(const int32_t* __restrict__ ti, int D, int64_t M, int m, int Nt0, int Nt1,
-                                    int Nt2, int bs0, int bs1, int bs2, int nt0, int nt1,
-                                    const int32_t* __restrict__ eoff, uint32_t* __restrict__ ekey,
-                                    int32_t* __restrict__ eval, int32_t* __restrict__ tcount) {
-  int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (i >= M) return;
-  const int Nt[3] = {Nt0, Nt1, Nt2};
-  const int bs[3] = {bs0, bs1, bs2};
-  int tl[3][kMaxL];
-  int n[3] = {1, 1, 1};
-  tl[1][0] = 0;
-  tl[2][0] = 0;
-  for (int d = 0; d < D; ++d) n[d] = tiles_touched(ti[int64_t(d) * M + i], m, Nt[d], bs[d], tl[d]);
-  int pos = eoff[i];
-  for (int c = 0; c < n[2]; ++c)
-    for (int b = 0; b < n[1]; ++b)
-      for (int a = 0; a < n[0]; ++a) {
-        uint32_t tile = uint32_t(tl[0][a] + nt0 * (tl[1][b] + nt1 * tl[2][c]));
-        ekey[pos] = tile;
-        eval[pos] = int32_t(i);
-        atomicAdd(&tcount[tile], 1);
-        ++pos;
-      }
-}
-
+// ------------------------------------------------------- spreading tasks
+// One task per chunk of at most `chunk` nodes of a non-empty home tile.
 __global__ void task_counts_kernel(const int32_t* __restrict__ tstart, int64_t ntiles, int chunk,
                                    int32_t* __restrict__ tcnt) {
   int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   if (t >= ntiles) return;
-  int n = tstart[t + 1] - tstart[t];
-  tcnt[t] = n == 0 ? 1 : (n + chunk - 1) / chunk;
+  const int n = tstart[t + 1] - tstart[t];
+  tcnt[t] = (n + chunk - 1) / chunk;
 }
 
 __global__ void fill_tasks_kernel(const int32_t* __restrict__ tstart, const int32_t* __restrict__ toff,
-                                  int64_t ntiles, int chunk, int4* __restrict__ tasks,
-                                  int32_t* __restrict__ multi, int* __restrict__ nmulti) {
+                                  int64_t ntiles, int chunk, int4* __restrict__ tasks) {
   int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   if (t >= ntiles) return;
   const int s = tstart[t], e = tstart[t + 1];
-  const int n = e - s;
-  const int nc = n == 0 ? 1 : (n + chunk - 1) / chunk;
   int pos = toff[t];
-  for (int c = 0; c < nc; ++c) {
-    int b = s + c * chunk;
-    int en = min(e, b + chunk);
-    tasks[pos + c] = make_int4(int(t), b, en, nc > 1 ? 1 : 0);
-  }
-  if (nc > 1) multi[atomicAdd(nmulti, 1)] = int(t);
+  for (int b = s; b < e; b += chunk) tasks[pos++] = make_int4(int(t), b, min(e, b + chunk), 0);
 }
 
 }  // namespace
@@ -276,17 +237,31 @@ int launch_reduce_nodes(const nfft_plan* p, const void* k, int32_t* ti_u, void* 
 }
 
 template <typename T>
-static int gather_sorted_t(const nfft_plan* p, const int32_t* perm, const int32_t* ti_u, const void* te_u) {
+static int node_tables_t(const nfft_plan* p, const int32_t* perm, const int32_t* ti_u, const void* te_u) {
   if (p->M == 0) return NFFT_OK;
-  gather_sorted_kernel<T><<<unsigned((p->M + 255) / 256), 256, 0, p->stream>>>(
-      perm, p->D, p->M, ti_u, static_cast<const T*>(te_u), p->ti, static_cast<T*>(p->te));
+  build_node_tables_kernel<T><<<unsigned((p->M + 255) / 256), 256, 0, p->stream>>>(
+      perm, p->D, p->M, ti_u, static_cast<const T*>(te_u), p->node4, static_cast<T*>(p->frac4));
   NFFT_LAUNCH_CHECK();
   return NFFT_OK;
 }
 
-int launch_gather_sorted(const nfft_plan* p, const int32_t* perm, const int32_t* ti_u, const void* te_u) {
-  return p->precision == 32 ? gather_sorted_t<float>(p, perm, ti_u, te_u)
-                            : gather_sorted_t<double>(p, perm, ti_u, te_u);
+int launch_build_node_tables(const nfft_plan* p, const int32_t* perm, const int32_t* ti_u, const void* te_u) {
+  return p->precision == 32 ? node_tables_t<float>(p, perm, ti_u, te_u) : node_tables_t<double>(p, perm, ti_u, te_u);
+}
+
+template <typename T> static int weight_table_t(const nfft_plan* p) {
+  const int64_t total = p->M * p->D * 2 * p->m;
+  if (total == 0) return NFFT_OK;
+  int64_t blocks = (total + 255) / 256;
+  if (blocks > 152 * 64) blocks = 152 * 64;
+  build_weight_table_kernel<T><<<unsigned(blocks), 256, 0, p->stream>>>(
+      make_geom<T>(p), static_cast<const T*>(p->frac4), p->M, static_cast<T*>(p->wtab));
+  NFFT_LAUNCH_CHECK();
+  return NFFT_OK;
+}
+
+int launch_build_weight_table(const nfft_plan* p) {
+  return p->precision == 32 ? weight_table_t<float>(p) : weight_table_t<double>(p);
 }
 
 int launch_deconv_factors(nfft_plan* p) {
@@ -303,42 +278,22 @@ int launch_deconv_factors(nfft_plan* p) {
   return NFFT_OK;
 }
 
-int launch_count_entries(const nfft_plan* p, int32_t* ecount) {
-  if (p->M == 0) return NFFT_OK;
-  count_entries_kernel<<<unsigned((p->M + 255) / 256), 256, 0, p->stream>>>(
-      p->ti, p->D, p->M, p->m, int(p->Nt[0]), int(p->Nt[1]), int(p->Nt[2]), int(p->bs[0]), int(p->bs[1]),
-      int(p->bs[2]), ecount);
-  NFFT_LAUNCH_CHECK();
-  return NFFT_OK;
-}
-
-int launch_fill_entries(const nfft_plan* p, const int32_t* eoff, uint32_t* ekey, int32_t* eval, int32_t* tcount) {
-  if (p->M == 0) return NFFT_OK;
-  fill_entries_kernel<<<unsigned((p->M + 255) / 256), 256, 0, p->stream>>>(
-      p->ti, p->D, p->M, p->m, int(p->Nt[0]), int(p->Nt[1]), int(p->Nt[2]), int(p->bs[0]), int(p->bs[1]),
-      int(p->bs[2]), int(p->ntiles[0]), int(p->ntiles[1]), eoff, ekey, eval, tcount);
-  NFFT_LAUNCH_CHECK();
-  return NFFT_OK;
-}
-
-// Chunk the tiles' entry ranges into spreading tasks.  tile_estart holds
-// ntiles+1 offsets on the device.  Allocates p->tasks and p->multi_tiles.
-int launch_build_tasks(nfft_plan* p, const int32_t* tile_estart, int chunk) {
+// Chunk the non-empty home tiles (CSR p->tile_start) into spreading tasks of
+// at most `chunk` nodes.  Allocates p->tasks.
+int launch_build_tasks(nfft_plan* p, int chunk) {
   const int64_t nt = p->ntiles_total;
   int32_t *tcnt = nullptr, *toff = nullptr;
   void* scr = nullptr;
-  int* nmulti = nullptr;
   int rc = NFFT_OK;
   const size_t sb = scan_scratch_bytes(nt + 1);
   if (cudaMalloc(&tcnt, sizeof(int32_t) * (nt + 1)) != cudaSuccess ||
-      cudaMalloc(&toff, sizeof(int32_t) * (nt + 1)) != cudaSuccess || cudaMalloc(&scr, sb) != cudaSuccess ||
-      cudaMalloc(&nmulti, sizeof(int)) != cudaSuccess) {
+      cudaMalloc(&toff, sizeof(int32_t) * (nt + 1)) != cudaSuccess || cudaMalloc(&scr, sb) != cudaSuccess) {
     set_error("cudaMalloc failed while building spreading tasks");
     rc = NFFT_ERR_ALLOC;
   }
-  int32_t ntasks = 0, nm = 0;
+  int32_t ntasks = 0;
   if (!rc) {
-    task_counts_kernel<<<unsigned((nt + 255) / 256), 256, 0, p->stream>>>(tile_estart, nt, chunk, tcnt);
+    task_counts_kernel<<<unsigned((nt + 255) / 256), 256, 0, p->stream>>>(p->tile_start, nt, chunk, tcnt);
     g_launches.fetch_add(1);
     cudaMemsetAsync(tcnt + nt, 0, sizeof(int32_t), p->stream);
     rc = exclusive_scan_i32(tcnt, toff, nt + 1, scr, sb, p->stream);
@@ -352,29 +307,22 @@ int launch_build_tasks(nfft_plan* p, const int32_t* tile_estart, int chunk) {
   }
   if (!rc) {
     p->n_tasks = ntasks;
-    if (cudaMalloc(&p->tasks, sizeof(int4) * size_t(ntasks > 0 ? ntasks : 1)) != cudaSuccess ||
-        cudaMalloc(&p->multi_tiles, sizeof(int32_t) * size_t(nt > 0 ? nt : 1)) != cudaSuccess) {
+    if (cudaMalloc(&p->tasks, sizeof(int4) * size_t(ntasks > 0 ? ntasks : 1)) != cudaSuccess) {
       set_error("cudaMalloc failed for spreading tasks");
       rc = NFFT_ERR_ALLOC;
     }
   }
-  if (!rc) {
-    p->scratch_bytes += sizeof(int4) * size_t(ntasks) + sizeof(int32_t) * size_t(nt);
-    cudaMemsetAsync(nmulti, 0, sizeof(int), p->stream);
-    fill_tasks_kernel<<<unsigned((nt + 255) / 256), 256, 0, p->stream>>>(tile_estart, toff, nt, chunk, p->tasks,
-                                                                         p->multi_tiles, nmulti);
+  if (!rc && ntasks > 0) {
+    fill_tasks_kernel<<<unsigned((nt + 255) / 256), 256, 0, p->stream>>>(p->tile_start, toff, nt, chunk, p->tasks);
     g_launches.fetch_add(1);
-    cudaMemcpyAsync(&nm, nmulti, sizeof(int), cudaMemcpyDeviceToHost, p->stream);
     if (cudaStreamSynchronize(p->stream) != cudaSuccess || cudaGetLastError() != cudaSuccess) {
       set_error("building spreading tasks failed");
       rc = NFFT_ERR_CUDA;
     }
-    p->n_multi = nm;
   }
   cudaFree(tcnt);
   cudaFree(toff);
   cudaFree(scr);
-  cudaFree(nmulti);
   return rc;
 }
 

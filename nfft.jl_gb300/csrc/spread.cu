@@ -1,200 +1,260 @@
 // Spreading (convolve_transpose!): g[tap] += prod_d phi_d * fHat[j] over the
 // (2m)^D window taps of every node, src/convolution.jl:349-520.
 //
-// Owner-computes tiles.  The grid is cut into tiles of bs[0] x bs[1] x bs[2]
-// points; nfft_set_nodes lists, for every tile, the (bin-sorted) nodes whose
-// window touches it and splits long lists into tasks.  One CTA per task:
-//   1. zero the tile accumulator in shared memory;
-//   2. stage a batch of nodes: per node and dimension, the 2m window values
-//      and the tile-local coordinate of each tap (-1 when the tap falls
-//      outside the tile, which also encodes periodic wrap-around);
-//   3. each warp spreads whole nodes, lane = (tap along dim 1, row slot),
-//      accumulating into the tile with shared-memory atomics;
-//   4. write the tile to the grid once with plain coalesced stores (tiles
-//      with a single task: no zero fill of the grid and no global atomics),
-//      or add it with global atomics (tiles split over several tasks, whose
-//      region was zeroed first).
-#include "nfft_internal.cuh"
+// The GB300 form of NFFT.jl's blocked adjoint (private padded block per
+// block, then a locked wrap-add into g, :356-443):
+//   * nodes are bin-sorted by home tile (bs[0] x bs[1] x bs[2] grid points);
+//     one CTA per task = one home tile or a chunk of a hot tile;
+//   * the CTA accumulates into the tile padded by 2m-1 points in shared
+//     memory (re and im planes, row pitch chosen so that the lanes of one
+//     warp step hit distinct banks), so every tap of every node lands inside
+//     it: no per-tap bounds tests and no wrap-around in the hot loop;
+//   * a warp spreads one node at a time (32/G nodes for D = 1) with shared-
+//     memory atomics, window values shuffled between lanes;
+//   * the padded tile is added to the zeroed grid with vector global atomics
+//     (red.global.add.v2), wrapping periodically; all-zero points are skipped.
+// The lock of the reference becomes the L2 atomics of the flush.
+#include "warpnode.cuh"
 
 namespace nfft {
 namespace {
 
 constexpr int kSpreadThreads = 256;
-constexpr int kStage = 32;  // nodes staged per batch
 
-template <int D, int L, typename T>
-struct Stage {
-  int16_t loc[kStage][D][L];
-  T w[kStage][D][L];
-  T cr[kStage];
-  T ci[kStage];
-};
-
-template <int D, int L, typename T>
-__device__ __forceinline__ void stage_nodes(const Geom<T>& G, const Nodes<T>& Nd, const T* cs, const int32_t* entries,
-                                            int eb, int ee, const int lo[3], const int ext[3], const T* fhat,
-                                            Stage<D, L, T>& S) {
-  const int n = ee - eb;
-  for (int q = threadIdx.x; q < kStage * D * L; q += blockDim.x) {
-    const int s = q / (D * L);
-    const int r = q - s * (D * L);
-    const int d = r / L;
-    const int l = r - d * L;
-    if (s < n) {
-      const int i = entries[eb + s];
-      const int t = Nd.ti[int64_t(d) * Nd.M + i];
-      const T e = Nd.te[int64_t(d) * Nd.M + i];
-      S.w[s][d][l] = tap_weight<T>(G, cs, e, l);
-      const int gg = G.small_grid ? wrap_any(t - G.m + 1 + l, G.Nt[d]) : wrap_once(t - G.m + 1 + l, G.Nt[d]);
-      const int lc = gg - lo[d];
-      S.loc[s][d][l] = int16_t((lc >= 0 && lc < ext[d]) ? lc : -1);
-    } else {
-      S.w[s][d][l] = T(0);
-      S.loc[s][d][l] = -1;
-    }
-  }
-  for (int s = threadIdx.x; s < kStage; s += blockDim.x) {
-    if (s < n) {
-      const int64_t j = Nd.perm[entries[eb + s]];
-      S.cr[s] = fhat[2 * j];
-      S.ci[s] = fhat[2 * j + 1];
-    } else {
-      S.cr[s] = T(0);
-      S.ci[s] = T(0);
-    }
-  }
+template <typename T> __device__ __forceinline__ void red_add2(T* g, T x, T y);
+template <> __device__ __forceinline__ void red_add2<float>(float* g, float x, float y) {
+  atomicAdd(reinterpret_cast<float2*>(g), make_float2(x, y));
+}
+template <> __device__ __forceinline__ void red_add2<double>(double* g, double x, double y) {
+  atomicAdd(g, x);
+  atomicAdd(g + 1, y);
 }
 
-template <int D, int L, typename T>
-__global__ void __launch_bounds__(kSpreadThreads) spread_tile_kernel(Geom<T> G, Nodes<T> Nd,
-                                                                      const int4* __restrict__ tasks,
-                                                                      const int32_t* __restrict__ entries,
-                                                                      const T* __restrict__ fhat,
-                                                                      T* __restrict__ g) {
-  constexpr int RY = (D == 1) ? 1 : (32 / L);
-  constexpr int NSTEP = (D == 1) ? 1 : (L + RY - 1) / RY;
+template <int D, int L, typename T, bool TABLE>
+__global__ void __launch_bounds__(kSpreadThreads) spread_pad_kernel(Geom<T> G, Nodes<T> Nd,
+                                                                     const int4* __restrict__ tasks,
+                                                                     const typename Cplx<T>::type* __restrict__ fhat,
+                                                                     T* __restrict__ g, int pitch) {
+  using C = typename Cplx<T>::type;
+  using LN = Lanes<D, L>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  __shared__ T cs[kMaxDeg * kMaxL];
-  __shared__ Stage<D, L, T> S;
   const int4 task = tasks[blockIdx.x];
   const int tile = task.x;
-  const int tcoord[3] = {tile % G.ntiles[0], (tile / G.ntiles[0]) % G.ntiles[1], tile / (G.ntiles[0] * G.ntiles[1])};
-  int lo[3], ext[3];
-#pragma unroll
-  for (int d = 0; d < 3; ++d) {
-    lo[d] = tcoord[d] * G.bs[d];
-    ext[d] = min(G.bs[d], G.Nt[d] - lo[d]);
+  const int tc0 = tile % G.ntiles[0];
+  const int tc1 = (tile / G.ntiles[0]) % G.ntiles[1];
+  const int tc2 = tile / (G.ntiles[0] * G.ntiles[1]);
+  // padded extents and origin (grid coordinate of padded index 0)
+  const int P0 = G.bs[0] + L - 1;
+  const int P1 = D >= 2 ? G.bs[1] + L - 1 : 1;
+  const int P2 = D >= 3 ? G.bs[2] + L - 1 : 1;
+  const int o0 = tc0 * G.bs[0], o1 = tc1 * G.bs[1], o2 = tc2 * G.bs[2];
+  const int plane = pitch * P1;
+  const int nwords = plane * P2;
+  T* sre = reinterpret_cast<T*>(smem_raw);
+  T* sim = sre + nwords;
+  for (int q = threadIdx.x; q < nwords; q += blockDim.x) {
+    sre[q] = T(0);
+    sim[q] = T(0);
   }
-  const int bs0 = G.bs[0], bs01 = G.bs[0] * G.bs[1];
-  const int npts = G.bs[0] * G.bs[1] * G.bs[2];
-  T* acc_r = reinterpret_cast<T*>(smem_raw);
-  T* acc_i = acc_r + npts;
-  for (int q = threadIdx.x; q < npts; q += blockDim.x) {
-    acc_r[q] = T(0);
-    acc_i[q] = T(0);
-  }
-  if (G.mode == WIN_POLY) {
-    const int n = (2 * G.m + 1) * L;
-    for (int q = threadIdx.x; q < n; q += blockDim.x) cs[q] = G.coeffs[q];
-  }
-  __syncthreads();
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
-  const int ix = lane % L;
-  const int ry = lane / L;
-  const bool xact = (D == 1) ? (lane < L) : (ry < RY);
-  for (int eb = task.y; eb < task.z; eb += kStage) {
-    const int ee = min(task.z, eb + kStage);
-    stage_nodes<D, L, T>(G, Nd, cs, entries, eb, ee, lo, ext, fhat, S);
-    __syncthreads();
-    const int n = ee - eb;
-    for (int s = warp; s < n; s += nwarps) {
-      const int lx = xact ? int(S.loc[s][0][ix]) : -1;
-      const T wx = S.w[s][0][ix];
-      const T cr = S.cr[s] * wx, ci = S.ci[s] * wx;
-      if constexpr (D == 1) {
-        if (lx >= 0) {
-          atomicAdd(acc_r + lx, cr);
-          atomicAdd(acc_i + lx, ci);
+  __syncthreads();
+
+  if constexpr (D == 1) {
+    const int slot = lane / LN::G1, ix = lane % LN::G1;
+    const bool act = ix < L;
+    T c[LN::DEG];
+    if constexpr (!TABLE) {
+#pragma unroll
+      for (int q = 0; q < LN::DEG; ++q) c[q] = act ? __ldg(G.coeffs + ix * LN::DEG + q) : T(0);
+    }
+    for (int b = task.y + warp * LN::NPW; b < task.z; b += nwarps * LN::NPW) {
+      const int i = b + slot;
+      if (i < task.z && act) {
+        const int4 nd = __ldg(Nd.node4 + i);
+        T w;
+        if constexpr (TABLE) {
+          w = __ldg(Nd.wtab + int64_t(i) * L + ix);
+        } else {
+          const T t = __ldg(Nd.frac4 + 4 * int64_t(i)) - T(0.5);
+          w = c[LN::DEG - 1];
+#pragma unroll
+          for (int q = LN::DEG - 2; q >= 0; --q) w = fma(w, t, c[q]);
+        }
+        const C v = __ldg(fhat + nd.w);
+        const int px = nd.x - o0 + ix;  // padded index of this tap
+        atomicAdd(sre + px, w * v.x);
+        atomicAdd(sim + px, w * v.y);
+      }
+    }
+  } else {
+    PolyRegs<D, L, T> P;
+    if constexpr (!TABLE) P.load(G.coeffs, lane);
+    const int ix = lane % L, ry = lane / L;
+    const bool xact = ry < LN::RY;
+    for (int i = task.y + warp; i < task.z; i += nwarps) {
+      const int4 nd = __ldg(Nd.node4 + i);
+      T W[LN::NW];
+      node_weights<D, L, T, TABLE>(Nd, P, i, lane, W);
+      const C v = __ldg(fhat + nd.w);
+      const T wx = wsel<D, L>(W, ix);
+      const T cr = v.x * wx, ci = v.y * wx;
+      const int px = nd.x - o0 + ix;
+      const int py0 = nd.y - o1;
+      int base[LN::NSTEP];
+      T vr[LN::NSTEP], vi[LN::NSTEP];
+      bool ok[LN::NSTEP];
+#pragma unroll
+      for (int s = 0; s < LN::NSTEP; ++s) {
+        const int iy = s * LN::RY + ry;
+        ok[s] = xact && iy < L;
+        const int iyc = ok[s] ? iy : 0;
+        const T wy = wsel<D, L>(W, L + iyc);  // every lane shuffles
+        base[s] = px + pitch * (py0 + iyc);
+        vr[s] = cr * wy;
+        vi[s] = ci * wy;
+      }
+      if constexpr (D == 2) {
+#pragma unroll
+        for (int s = 0; s < LN::NSTEP; ++s) {
+          if (ok[s]) {
+            atomicAdd(sre + base[s], vr[s]);
+            atomicAdd(sim + base[s], vi[s]);
+          }
         }
       } else {
-        int rowoff[NSTEP];
-        T vr[NSTEP], vi[NSTEP];
+        const int pz0 = (nd.z - o2) * plane;
 #pragma unroll
-        for (int st = 0; st < NSTEP; ++st) {
-          const int iy = st * RY + ry;
-          const int ly = (lx >= 0 && iy < L) ? int(S.loc[s][1][iy < L ? iy : 0]) : -1;
-          const T wy = S.w[s][1][iy < L ? iy : 0];
-          rowoff[st] = ly >= 0 ? lx + bs0 * ly : -1;
-          vr[st] = cr * wy;
-          vi[st] = ci * wy;
-        }
-        if constexpr (D == 2) {
+        for (int iz = 0; iz < L; ++iz) {
+          const T wz = wsel<D, L>(W, 2 * L + iz);
+          const int pz = pz0 + iz * plane;
 #pragma unroll
-          for (int st = 0; st < NSTEP; ++st) {
-            if (rowoff[st] >= 0) {
-              atomicAdd(acc_r + rowoff[st], vr[st]);
-              atomicAdd(acc_i + rowoff[st], vi[st]);
-            }
-          }
-        } else {
-#pragma unroll 2
-          for (int iz = 0; iz < L; ++iz) {
-            const int lz = S.loc[s][D - 1][iz];
-            if (lz < 0) continue;  // uniform across the warp
-            const T wz = S.w[s][D - 1][iz];
-            const int pz = lz * bs01;
-#pragma unroll
-            for (int st = 0; st < NSTEP; ++st) {
-              if (rowoff[st] >= 0) {
-                atomicAdd(acc_r + pz + rowoff[st], vr[st] * wz);
-                atomicAdd(acc_i + pz + rowoff[st], vi[st] * wz);
-              }
+          for (int s = 0; s < LN::NSTEP; ++s) {
+            if (ok[s]) {
+              atomicAdd(sre + pz + base[s], vr[s] * wz);
+              atomicAdd(sim + pz + base[s], vi[s] * wz);
             }
           }
         }
       }
     }
-    __syncthreads();
   }
-  // write the tile once
-  const bool multi = task.w != 0;
-  for (int q = threadIdx.x; q < npts; q += blockDim.x) {
-    const int x = q % G.bs[0];
-    const int y = (q / G.bs[0]) % G.bs[1];
-    const int z = q / bs01;
-    if (x >= ext[0] || y >= ext[1] || z >= ext[2]) continue;
-    const int64_t gi = int64_t(lo[0] + x) + int64_t(G.Nt[0]) * (int64_t(lo[1] + y) + int64_t(G.Nt[1]) * (lo[2] + z));
-    using C = typename Cplx<T>::type;
-    C v;
-    v.x = acc_r[q];
-    v.y = acc_i[q];
-    if (multi) {
-      atomicAdd(g + 2 * gi, v.x);
-      atomicAdd(g + 2 * gi + 1, v.y);
-    } else {
-      reinterpret_cast<C*>(g)[gi] = v;
+  __syncthreads();
+
+  // flush: padded point (x, y, z) -> grid ((o - m + 1 + x) mod Ntilde, ...)
+  const int m1 = G.m - 1;
+  const bool small = G.small_grid;
+  const int rows = P1 * P2;
+  for (int r = warp; r < rows; r += nwarps) {
+    const int y = r % P1, z = r / P1;
+    const int gy = D >= 2 ? (small ? wrap_any(o1 - m1 + y, G.Nt[1]) : wrap_once(o1 - m1 + y, G.Nt[1])) : 0;
+    const int gz = D >= 3 ? (small ? wrap_any(o2 - m1 + z, G.Nt[2]) : wrap_once(o2 - m1 + z, G.Nt[2])) : 0;
+    T* grow = g + 2 * (int64_t(gz) * G.plane + int64_t(gy) * G.Nt[0]);
+    const int srow = z * plane + y * pitch;
+    for (int x = lane; x < P0; x += 32) {
+      const T a = sre[srow + x], b = sim[srow + x];
+      if (a != T(0) || b != T(0)) {
+        const int gx = small ? wrap_any(o0 - m1 + x, G.Nt[0]) : wrap_once(o0 - m1 + x, G.Nt[0]);
+        red_add2<T>(grow + 2 * gx, a, b);
+      }
     }
   }
 }
 
-// Zero the tiles that several tasks add into.
-template <typename T>
-__global__ void zero_tiles_kernel(Geom<T> G, const int32_t* __restrict__ tiles, T* __restrict__ g) {
-  const int tile = tiles[blockIdx.x];
-  const int tc[3] = {tile % G.ntiles[0], (tile / G.ntiles[0]) % G.ntiles[1], tile / (G.ntiles[0] * G.ntiles[1])};
-  int lo[3], ext[3];
-  for (int d = 0; d < 3; ++d) {
-    lo[d] = tc[d] * G.bs[d];
-    ext[d] = min(G.bs[d], G.Nt[d] - lo[d]);
+// Compensated variant: warp w owns the slices of the padded tile along the
+// last dimension whose index is w mod (number of warps); a slice is an x-y
+// plane (D = 3), an x row (D = 2) or a point (D = 1).  Every point then has
+// one writer, which adds the node contributions in node order with Kahan
+// compensation (sum and compensation kept in shared memory).
+template <int D, int L, typename T, bool TABLE>
+__global__ void __launch_bounds__(kSpreadThreads) spread_kahan_kernel(Geom<T> G, Nodes<T> Nd,
+                                                                       const int4* __restrict__ tasks,
+                                                                       const typename Cplx<T>::type* __restrict__ fhat,
+                                                                       T* __restrict__ g, int pitch) {
+  using C = typename Cplx<T>::type;
+  using LN = Lanes<D, L>;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int4 task = tasks[blockIdx.x];
+  const int tile = task.x;
+  const int tc0 = tile % G.ntiles[0];
+  const int tc1 = (tile / G.ntiles[0]) % G.ntiles[1];
+  const int tc2 = tile / (G.ntiles[0] * G.ntiles[1]);
+  const int P0 = G.bs[0] + L - 1;
+  const int P1 = D >= 2 ? G.bs[1] + L - 1 : 1;
+  const int P2 = D >= 3 ? G.bs[2] + L - 1 : 1;
+  const int o0 = tc0 * G.bs[0], o1 = tc1 * G.bs[1], o2 = tc2 * G.bs[2];
+  const int plane = pitch * P1;
+  const int nwords = plane * P2;
+  T* sre = reinterpret_cast<T*>(smem_raw);
+  T* sim = sre + nwords;
+  T* cre = sim + nwords;
+  T* cim = cre + nwords;
+  for (int q = threadIdx.x; q < 4 * nwords; q += blockDim.x) sre[q] = T(0);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  __syncthreads();
+  PolyRegs<D, L, T> P;
+  if constexpr (!TABLE) P.load(G.coeffs, lane);
+  // lane layout inside a slice
+  const int ix = D == 1 ? 0 : lane % L;
+  const int ry = D == 3 ? lane / L : 0;
+  const bool xact = D == 1 ? lane == 0 : (D == 2 ? lane < L : ry < LN::RY);
+  constexpr int NST = D == 3 ? LN::NSTEP : 1;
+  auto kahan = [](T* s, T* c, int idx, T v) {
+    const T y = v - c[idx];
+    const T t = s[idx] + y;
+    c[idx] = (t - s[idx]) - y;
+    s[idx] = t;
+  };
+  for (int i = task.y; i < task.z; ++i) {
+    const int4 nd = __ldg(Nd.node4 + i);
+    const int tlast = D == 3 ? nd.z - o2 : (D == 2 ? nd.y - o1 : nd.x - o0);
+    // first of this node's slices owned by this warp
+    int is = (warp - tlast) % nwarps;
+    if (is < 0) is += nwarps;
+    if (is >= L) continue;  // uniform per warp: no slice of this node is owned
+    T W[LN::NW];
+    node_weights<D, L, T, TABLE>(Nd, P, i, lane, W);
+    const C v = __ldg(fhat + nd.w);
+    for (; is < L; is += nwarps) {
+      const T wl = wsel<D, L>(W, (D - 1) * L + is);
+      const T br = v.x * wl, bi = v.y * wl;
+      if constexpr (D == 1) {
+        if (lane == 0) kahan(sre, cre, tlast + is, br), kahan(sim, cim, tlast + is, bi);
+      } else if constexpr (D == 2) {
+        const T wx = wsel<D, L>(W, ix);
+        const int idx = (nd.y - o1 + is) * pitch + (nd.x - o0 + ix);
+        if (xact) kahan(sre, cre, idx, br * wx), kahan(sim, cim, idx, bi * wx);
+      } else {
+        const T wx = wsel<D, L>(W, ix);
+        const int pz = (nd.z - o2 + is) * plane;
+#pragma unroll
+        for (int s = 0; s < NST; ++s) {
+          const int iy = s * LN::RY + ry;
+          const bool ok = xact && iy < L;
+          const int iyc = ok ? iy : 0;
+          const T wy = wsel<D, L>(W, L + iyc);
+          const int idx = pz + (nd.y - o1 + iyc) * pitch + (nd.x - o0 + ix);
+          if (ok) kahan(sre, cre, idx, br * wx * wy), kahan(sim, cim, idx, bi * wx * wy);
+        }
+      }
+    }
   }
-  const int npts = ext[0] * ext[1] * ext[2];
-  for (int q = threadIdx.x; q < npts; q += blockDim.x) {
-    const int x = q % ext[0];
-    const int y = (q / ext[0]) % ext[1];
-    const int z = q / (ext[0] * ext[1]);
-    const int64_t gi = int64_t(lo[0] + x) + int64_t(G.Nt[0]) * (int64_t(lo[1] + y) + int64_t(G.Nt[1]) * (lo[2] + z));
-    g[2 * gi] = T(0);
-    g[2 * gi + 1] = T(0);
+  __syncthreads();
+  const int m1 = G.m - 1;
+  const bool small = G.small_grid;
+  const int rows = P1 * P2;
+  for (int r = warp; r < rows; r += nwarps) {
+    const int y = r % P1, z = r / P1;
+    const int gy = D >= 2 ? (small ? wrap_any(o1 - m1 + y, G.Nt[1]) : wrap_once(o1 - m1 + y, G.Nt[1])) : 0;
+    const int gz = D >= 3 ? (small ? wrap_any(o2 - m1 + z, G.Nt[2]) : wrap_once(o2 - m1 + z, G.Nt[2])) : 0;
+    T* grow = g + 2 * (int64_t(gz) * G.plane + int64_t(gy) * G.Nt[0]);
+    const int srow = z * plane + y * pitch;
+    for (int x = lane; x < P0; x += 32) {
+      const T a = sre[srow + x] - cre[srow + x], b = sim[srow + x] - cim[srow + x];
+      if (a != T(0) || b != T(0)) {
+        const int gx = small ? wrap_any(o0 - m1 + x, G.Nt[0]) : wrap_once(o0 - m1 + x, G.Nt[0]);
+        red_add2<T>(grow + 2 * gx, a, b);
+      }
+    }
   }
 }
 
@@ -202,60 +262,73 @@ template <int D, int L, typename T>
 int spread_launch(nfft_plan* p, const void* fhat, void* g) {
   Geom<T> G = make_geom<T>(p);
   Nodes<T> Nd = make_nodes<T>(p);
-  const size_t smem = size_t(2) * sizeof(T) * size_t(p->bs[0] * p->bs[1] * p->bs[2]);
-  auto kern = spread_tile_kernel<D, L, T>;
-  const size_t static_smem = sizeof(Stage<D, L, T>) + sizeof(T) * kMaxDeg * kMaxL;
-  if (smem + static_smem > 227 * 1024) {
-    set_error("spreading tile of %lld points does not fit in shared memory",
-              (long long)(p->bs[0] * p->bs[1] * p->bs[2]));
+  const size_t gbytes = size_t(p->Nt[0] * p->Nt[1] * p->Nt[2]) * sizeof(T) * 2;
+  NFFT_CUDA_TRY(cudaMemsetAsync(g, 0, gbytes, p->stream));
+  if (p->n_tasks == 0) return NFFT_OK;
+  const int P1 = D >= 2 ? int(p->bs[1]) + L - 1 : 1;
+  const int P2 = D >= 3 ? int(p->bs[2]) + L - 1 : 1;
+  const bool comp = p->prm.compensated != 0;
+  const size_t smem = size_t(comp ? 4 : 2) * sizeof(T) * size_t(p->spread_pitch) * P1 * P2;
+  if (smem > 227 * 1024) {
+    set_error("padded spreading tile (%zu bytes) does not fit in shared memory; use a smaller blockSize", smem);
     return NFFT_ERR_UNSUPPORTED;
   }
+  auto kern = comp ? (p->wtab ? spread_kahan_kernel<D, L, T, true> : spread_kahan_kernel<D, L, T, false>)
+                   : (p->wtab ? spread_pad_kernel<D, L, T, true> : spread_pad_kernel<D, L, T, false>);
   NFFT_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
-  if (p->n_multi > 0) {
-    zero_tiles_kernel<T><<<unsigned(p->n_multi), 256, 0, p->stream>>>(G, p->multi_tiles, static_cast<T*>(g));
-    NFFT_LAUNCH_CHECK();
-  }
-  if (p->n_tasks > 0) {
-    kern<<<unsigned(p->n_tasks), kSpreadThreads, smem, p->stream>>>(G, Nd, p->tasks, p->entries,
-                                                                   static_cast<const T*>(fhat), static_cast<T*>(g));
-    NFFT_LAUNCH_CHECK();
-  }
+  kern<<<unsigned(p->n_tasks), kSpreadThreads, smem, p->stream>>>(
+      G, Nd, p->tasks, static_cast<const typename Cplx<T>::type*>(fhat), static_cast<T*>(g), p->spread_pitch);
+  NFFT_LAUNCH_CHECK();
   return NFFT_OK;
 }
 
-template <int D, int L, typename T>
-int spread_dispatch_c(nfft_plan* p, const void* fhat, int, void* g, int) {
-  return spread_launch<D, L, T>(p, fhat, g);
-}
-
-template <int D, typename T> int spread_dispatch_l(nfft_plan* p, const void* fhat, int fr, void* g, int gr) {
+template <int D, typename T> int spread_dispatch_l(nfft_plan* p, const void* fhat, void* g) {
   switch (p->m) {
-    case 2: return spread_dispatch_c<D, 4, T>(p, fhat, fr, g, gr);
-    case 3: return spread_dispatch_c<D, 6, T>(p, fhat, fr, g, gr);
-    case 4: return spread_dispatch_c<D, 8, T>(p, fhat, fr, g, gr);
-    case 5: return spread_dispatch_c<D, 10, T>(p, fhat, fr, g, gr);
-    case 6: return spread_dispatch_c<D, 12, T>(p, fhat, fr, g, gr);
-    case 7: return spread_dispatch_c<D, 14, T>(p, fhat, fr, g, gr);
-    case 8: return spread_dispatch_c<D, 16, T>(p, fhat, fr, g, gr);
+    case 2: return spread_launch<D, 4, T>(p, fhat, g);
+    case 3: return spread_launch<D, 6, T>(p, fhat, g);
+    case 4: return spread_launch<D, 8, T>(p, fhat, g);
+    case 5: return spread_launch<D, 10, T>(p, fhat, g);
+    case 6: return spread_launch<D, 12, T>(p, fhat, g);
+    case 7: return spread_launch<D, 14, T>(p, fhat, g);
+    case 8: return spread_launch<D, 16, T>(p, fhat, g);
   }
   set_error("m = %d not supported (2..8)", p->m);
   return NFFT_ERR_UNSUPPORTED;
 }
 
-template <typename T> int spread_dispatch(nfft_plan* p, const void* fhat, int fr, void* g, int gr) {
+template <typename T> int spread_dispatch(nfft_plan* p, const void* fhat, void* g) {
   switch (p->D) {
-    case 1: return spread_dispatch_l<1, T>(p, fhat, fr, g, gr);
-    case 2: return spread_dispatch_l<2, T>(p, fhat, fr, g, gr);
-    case 3: return spread_dispatch_l<3, T>(p, fhat, fr, g, gr);
+    case 1: return spread_dispatch_l<1, T>(p, fhat, g);
+    case 2: return spread_dispatch_l<2, T>(p, fhat, g);
+    case 3: return spread_dispatch_l<3, T>(p, fhat, g);
   }
   return NFFT_ERR_UNSUPPORTED;
 }
 
 }  // namespace
 
-int launch_spread(nfft_plan* p, const void* fhat, int fhat_real, void* g, int g_real) {
-  return p->precision == 32 ? spread_dispatch<float>(p, fhat, fhat_real, g, g_real)
-                            : spread_dispatch<double>(p, fhat, fhat_real, g, g_real);
+// Row pitch (in elements) of the padded tile: the smallest pitch >= the
+// padded row length for which the lanes of one warp step (L taps along x
+// times RY rows) touch distinct shared-memory banks.
+int spread_pitch_for(int D, int m, int P0, int elem_bytes) {
+  const int L = 2 * m;
+  const int RY = D == 1 ? 1 : 32 / L;
+  const int words = elem_bytes / 4;
+  for (int pitch = P0; pitch < P0 + 64; ++pitch) {
+    int used[32] = {};
+    int worst = 0;
+    for (int ry = 0; ry < RY; ++ry)
+      for (int ix = 0; ix < L; ++ix) {
+        const int bank = ((ix + pitch * ry) * words) % 32;
+        worst = ++used[bank] > worst ? used[bank] : worst;
+      }
+    if (worst <= words) return pitch;
+  }
+  return P0;
+}
+
+int launch_spread(nfft_plan* p, const void* fhat, int, void* g, int) {
+  return p->precision == 32 ? spread_dispatch<float>(p, fhat, g) : spread_dispatch<double>(p, fhat, g);
 }
 
 }  // namespace nfft

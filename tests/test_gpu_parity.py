@@ -138,3 +138,29 @@ def test_plain_path_matches_oracle():
         y, x = gpu_fwd_adj(p, f, fhat)
         assert oracle.rel_l2(y, op.forward(f)) < TOL64
         assert oracle.rel_l2(colmajor_flat(x), colmajor_flat(op.adjoint(fhat))) < TOL64
+
+
+@pytest.mark.parametrize("D,N,M", [(1, (128,), 700), (2, (24, 20), 900), (3, (12, 10, 8), 1500)])
+@pytest.mark.parametrize("dtype", [np.float32, np.float64])
+def test_compensated_spreading_matches_oracle(D, N, M, dtype):
+    """Kahan-compensated spreading tiles (compensated=True) give the same
+    adjoint as the oracle: <= 1e-11 (FP64) / 1e-5 (FP32)."""
+    k, f, fhat = rand_problem(D, N, M, seed=31, dtype=dtype)
+    bs = {1: (64,), 2: (16, 16), 3: (8, 8, 8)}[D]
+    p = nf.plan_nfft(k, N, m=4, sigma=2.0, compensated=True, blockSize=bs)
+    op = oracle.OraclePlan(k.astype(np.float64), N, m=4, sigma=2.0)
+    x = (nf.adjoint(p) * torch.as_tensor(fhat).to(p.cdtype)).cpu().numpy()
+    tol = TOL64 if dtype == np.float64 else TOL32
+    assert oracle.rel_l2(colmajor_flat(x), colmajor_flat(op.adjoint(fhat))) < tol
+
+
+@pytest.mark.parametrize("pre", [oracle.POLYNOMIAL, oracle.TENSOR])
+def test_polynomial_and_tensor_agree(pre):
+    """POLYNOMIAL evaluates the fitted window per tap, TENSOR stores it at
+    nodes!: both equal the oracle's TENSOR plan."""
+    k, f, fhat = rand_problem(3, (16, 12, 10), 2500, seed=41)
+    p = nf.plan_nfft(k, (16, 12, 10), m=4, sigma=2.0, precompute=pre)
+    op = oracle.OraclePlan(k, (16, 12, 10), m=4, sigma=2.0, precompute=oracle.TENSOR)
+    y, x = gpu_fwd_adj(p, f, fhat)
+    assert oracle.rel_l2(y, op.forward(f)) < TOL64
+    assert oracle.rel_l2(colmajor_flat(x), colmajor_flat(op.adjoint(fhat))) < TOL64
