@@ -148,6 +148,23 @@ def rel_err_subset(k64, f, fhat, y, x, n_fwd=48, n_adj=24, seed=7):
     return e_fwd, e_adj
 
 
+def max_over_ranks(t, world, device):
+    """The slowest rank's time (replicas run independently; this is the only
+    collective, outside the data path)."""
+    if world <= 1:
+        return float(t)
+    import torch
+    import torch.distributed as dist
+    tt = torch.tensor([float(t)], dtype=torch.float64, device=device)
+    dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+    return float(tt.item())
+
+
+def aggregate_nodes_per_s(world, m_nodes, steps, t_max):
+    """Whole-job throughput: every rank processes its own replica."""
+    return world * m_nodes * steps / t_max
+
+
 def cpu_reference_run(steps, warmup, budget_s=150.0):
     """The oracle (FP32) on the host cores: full forward + adjoint steps."""
     from oracle import oracle
@@ -221,7 +238,10 @@ def run_ours(args):
     stats = nf.TimingStats()
     t0 = time.perf_counter()
     pre = {"tensor": nf.TENSOR, "polynomial": nf.POLYNOMIAL, "full": nf.FULL, "linear": nf.LINEAR}[args.precompute]
-    p = nf.plan_nfft(k, N3, m=4, sigma=2.0, window="kaiser_bessel", precompute=pre, timing=stats)
+    bs = tuple(int(v) for v in args.blocksize.split(",")) if args.blocksize else None
+    p = nf.plan_nfft(k, N3, m=4, sigma=2.0, window="kaiser_bessel", precompute=pre, timing=stats, blockSize=bs)
+    if args.autotune:
+        p.autotune(use_cache=True)
     torch.cuda.synchronize()
     t_pre = time.perf_counter() - t0
     f = nf.as_colmajor(f_h, N3, torch.complex64, dev)
@@ -253,12 +273,8 @@ def run_ours(args):
         if world > 1:
             dist.barrier()
     launches = nf.kernel_launch_count() - launches0
-    t_dev = ev0.elapsed_time(ev1) * 1e-3
-    if world > 1:
-        tt = torch.tensor([t_dev], device=dev, dtype=torch.float64)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t_dev = float(tt.item())
-    value = world * M_NODES * args.steps / t_dev
+    t_dev = max_over_ranks(ev0.elapsed_time(ev1) * 1e-3, world, dev)
+    value = aggregate_nodes_per_s(world, M_NODES, args.steps, t_dev)
 
     import ctypes
     tot = (ctypes.c_double * 7)()
@@ -299,12 +315,8 @@ def run_ours(args):
         e2e_step()
     e1.record(stream)
     torch.cuda.synchronize()
-    t_e2e = e0.elapsed_time(e1) * 1e-3
-    if world > 1:
-        tt = torch.tensor([t_e2e], device=dev, dtype=torch.float64)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t_e2e = float(tt.item())
-    e2e_value = world * M_NODES * e2e_steps / t_e2e
+    t_e2e = max_over_ranks(e0.elapsed_time(e1) * 1e-3, world, dev)
+    e2e_value = aggregate_nodes_per_s(world, M_NODES, e2e_steps, t_e2e)
     h2d = f_pin.numel() * 8 + fhat_pin.numel() * 8
     d2h = y_pin.numel() * 8 + x_pin.numel() * 8
 
@@ -379,6 +391,7 @@ def run_ours(args):
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": WORKLOAD, "precision": "FP32 (FP64 node reduction and deconvolution factors)",
                        "precompute": args.precompute.upper(),
+                       "block_size": list(p.params.blockSize),
                        "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
                        "l2": "inputs larger than L2 (grid 1.07 GB, image 134 MB); no extra flush",
                        "plan_seconds": t_pre},
@@ -407,6 +420,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--precompute", default="tensor", choices=["tensor", "polynomial", "full", "linear"],
                     help="window evaluation of the plan (PrecomputeFlags)")
+    ap.add_argument("--blocksize", default=None, help="spreading tile, e.g. 16,8,8 (NFFTParams.blockSize)")
+    ap.add_argument("--autotune", type=int, default=1, help="1: pick the tile with the library's autotuner")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-check", action="store_true")

@@ -177,6 +177,18 @@ int nfft_deconvolve_transpose(nfft_plan* plan, const void* g, void* f);
  * (v, w) = (xbar, y). */
 int nfft_grad_nodes(nfft_plan* plan, const void* v, const void* w, void* dk);
 
+/* Tile-shape autotuner (no reference counterpart; the reference's blockSize
+ * keyword is chosen by hand, src/precomputation.jl:59-77).  Re-bins the
+ * plan's nodes for a set of candidate tile shapes, times one spreading and
+ * one gather pass per candidate on the plan's stream, and keeps the fastest.
+ * With use_cache = 1 the choice is looked up in / stored to the file named by
+ * the environment variable NFFT_GB300_TUNE_CACHE, keyed by (D, Ntilde,
+ * log2 M, m, precision, SM count, precompute, compensated).  Synchronises. */
+int nfft_autotune(nfft_plan* plan, int use_cache);
+
+/* Re-tile the plan (blockSize) and re-bin its nodes.  Synchronises. */
+int nfft_set_block_size(nfft_plan* plan, const int64_t* block_size);
+
 /* Plan geometry and sizes. */
 int nfft_get_info(const nfft_plan* plan, nfft_info* info);
 

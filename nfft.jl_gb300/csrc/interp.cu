@@ -129,6 +129,145 @@ __global__ void __launch_bounds__(kInterpThreads) interp_kernel(Geom<T> G, Nodes
   }
 }
 
+// Tile-staged gather: one CTA per spreading task (home tile or chunk of a hot
+// tile).  The CTA copies the tile's padded neighbourhood of the grid (with
+// periodic wrap) into shared memory with coalesced row loads, then each warp
+// interpolates one node at a time from shared memory: no wrap logic and no
+// global addressing in the tap loop.
+template <int D, int L, typename T, bool TABLE>
+__global__ void __launch_bounds__(kInterpThreads) interp_tile_kernel(Geom<T> G, Nodes<T> Nd,
+                                                                      const int4* __restrict__ tasks,
+                                                                      const typename Cplx<T>::type* __restrict__ g,
+                                                                      typename Cplx<T>::type* __restrict__ fhat,
+                                                                      int pitch) {
+  using C = typename Cplx<T>::type;
+  using LN = Lanes<D, L>;
+  extern __shared__ __align__(32) unsigned char smem_raw[];
+  C* tile = reinterpret_cast<C*>(smem_raw);
+  const int4 task = tasks[blockIdx.x];
+  const int t = task.x;
+  const int tc0 = t % G.ntiles[0];
+  const int tc1 = (t / G.ntiles[0]) % G.ntiles[1];
+  const int tc2 = t / (G.ntiles[0] * G.ntiles[1]);
+  const int P0 = G.bs[0] + L - 1;
+  const int P1 = D >= 2 ? G.bs[1] + L - 1 : 1;
+  const int P2 = D == 3 ? G.bs[2] + L - 1 : 1;
+  const int o0 = tc0 * G.bs[0], o1 = D >= 2 ? tc1 * G.bs[1] : 0, o2 = D == 3 ? tc2 * G.bs[2] : 0;
+  const int plane = pitch * P1;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  const int m1 = G.m - 1;
+  const bool small = G.small_grid;
+  // stage the padded tile
+  for (int r = warp; r < P1 * P2; r += nwarps) {
+    const int y = r % P1, z = r / P1;
+    const int gy = D >= 2 ? (small ? wrap_any(o1 - m1 + y, G.Nt[1]) : wrap_once(o1 - m1 + y, G.Nt[1])) : 0;
+    const int gz = D == 3 ? (small ? wrap_any(o2 - m1 + z, G.Nt[2]) : wrap_once(o2 - m1 + z, G.Nt[2])) : 0;
+    const C* grow = g + int64_t(gz) * G.plane + int64_t(gy) * G.Nt[0];
+    C* srow = tile + z * plane + y * pitch;
+    for (int x = lane; x < P0; x += 32) {
+      const int gx = small ? wrap_any(o0 - m1 + x, G.Nt[0]) : wrap_once(o0 - m1 + x, G.Nt[0]);
+      srow[x] = __ldg(grow + gx);
+    }
+  }
+  __syncthreads();
+  if constexpr (D == 1) {
+    const int slot = lane / LN::G1, ix = lane % LN::G1;
+    const bool act = ix < L;
+    T c[LN::DEG];
+    if constexpr (!TABLE) {
+#pragma unroll
+      for (int q = 0; q < LN::DEG; ++q) c[q] = act ? __ldg(G.coeffs + ix * LN::DEG + q) : T(0);
+    }
+    for (int b = task.y + warp * LN::NPW; b < task.z; b += nwarps * LN::NPW) {
+      const int i = b + slot;
+      T ar = T(0), ai = T(0);
+      int4 nd = make_int4(0, 0, 0, 0);
+      if (i < task.z) nd = __ldg(Nd.node4 + i);
+      if (i < task.z && act) {
+        T w;
+        if constexpr (TABLE) {
+          w = __ldg(Nd.wtab + int64_t(i) * L + ix);
+        } else {
+          const T tt = __ldg(Nd.frac4 + 4 * int64_t(i)) - T(0.5);
+          w = c[LN::DEG - 1];
+#pragma unroll
+          for (int q = LN::DEG - 2; q >= 0; --q) w = fma(w, tt, c[q]);
+        }
+        const C v = tile[nd.x - o0 + ix];
+        ar = w * v.x;
+        ai = w * v.y;
+      }
+#pragma unroll
+      for (int o = LN::G1 / 2; o > 0; o >>= 1) {
+        ar += __shfl_xor_sync(0xFFFFFFFFu, ar, o);
+        ai += __shfl_xor_sync(0xFFFFFFFFu, ai, o);
+      }
+      if (ix == 0 && i < task.z) {
+        C r;
+        r.x = ar;
+        r.y = ai;
+        fhat[nd.w] = r;
+      }
+    }
+  } else {
+    PolyRegs<D, L, T> P;
+    if constexpr (!TABLE) P.load(G.coeffs, lane);
+    const int ix = lane % L, ry = lane / L;
+    const bool xact = ry < LN::RY;
+    for (int i = task.y + warp; i < task.z; i += nwarps) {
+      const int4 nd = __ldg(Nd.node4 + i);
+      T W[LN::NW];
+      node_weights<D, L, T, TABLE>(Nd, P, i, lane, W);
+      const T wx = wsel<D, L>(W, ix);
+      const int px = nd.x - o0 + ix, py = nd.y - o1;
+      int row[LN::NSTEP];
+      T wxy[LN::NSTEP];
+#pragma unroll
+      for (int s = 0; s < LN::NSTEP; ++s) {
+        const int iy = s * LN::RY + ry;
+        const bool ok = xact && iy < L;
+        const int iyc = ok ? iy : 0;
+        const T wy = wsel<D, L>(W, L + iyc);  // every lane shuffles
+        row[s] = (py + iyc) * pitch + px;
+        wxy[s] = ok ? wx * wy : T(0);
+      }
+      T ar = T(0), ai = T(0);
+      if constexpr (D == 2) {
+#pragma unroll
+        for (int s = 0; s < LN::NSTEP; ++s) {
+          const C v = tile[row[s]];
+          ar = fma(wxy[s], v.x, ar);
+          ai = fma(wxy[s], v.y, ai);
+        }
+      } else {
+        const C* pl = tile + (nd.z - o2) * plane;
+#pragma unroll
+        for (int iz = 0; iz < L; ++iz) {
+          const T wz = wsel<D, L>(W, 2 * L + iz);
+#pragma unroll
+          for (int s = 0; s < LN::NSTEP; ++s) {
+            const C v = pl[iz * plane + row[s]];
+            const T w = wxy[s] * wz;
+            ar = fma(w, v.x, ar);
+            ai = fma(w, v.y, ai);
+          }
+        }
+      }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        ar += __shfl_xor_sync(0xFFFFFFFFu, ar, o);
+        ai += __shfl_xor_sync(0xFFFFFFFFu, ai, o);
+      }
+      if (lane == 0) {
+        C r;
+        r.x = ar;
+        r.y = ai;
+        fhat[nd.w] = r;
+      }
+    }
+  }
+}
+
 template <int D, int L, typename T>
 int interp_launch(const nfft_plan* p, const void* g, void* fhat) {
   Geom<T> G = make_geom<T>(p);
@@ -141,6 +280,18 @@ int interp_launch(const nfft_plan* p, const void* g, void* fhat) {
   if (blocks > cap) blocks = cap;
   const C* gp = static_cast<const C*>(g);
   C* fp = static_cast<C*>(fhat);
+  if (p->tasks && p->gather_tiled) {
+    const int P1 = D >= 2 ? int(p->bs[1]) + L - 1 : 1;
+    const int P2 = D == 3 ? int(p->bs[2]) + L - 1 : 1;
+    const size_t smem = sizeof(C) * size_t(p->gather_pitch) * P1 * P2;
+    if (smem <= 227 * 1024 && p->n_tasks > 0) {
+      auto kern = p->wtab ? interp_tile_kernel<D, L, T, true> : interp_tile_kernel<D, L, T, false>;
+      NFFT_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
+      kern<<<unsigned(p->n_tasks), kInterpThreads, smem, p->stream>>>(G, Nd, p->tasks, gp, fp, p->gather_pitch);
+      NFFT_LAUNCH_CHECK();
+      return NFFT_OK;
+    }
+  }
   if (p->wtab)
     interp_kernel<D, L, T, true><<<unsigned(blocks), kInterpThreads, 0, p->stream>>>(G, Nd, gp, fp);
   else

@@ -94,8 +94,17 @@ struct nfft_plan {
   int64_t ntiles[3] = {1, 1, 1};
   int64_t ntiles_total = 1;
   cudaStream_t stream = nullptr;
-  cufftHandle fft = 0;
-  bool fft_ok = false;
+  // FFT of the oversampled grid.  D = 1: one plan.  D >= 2 (pruned): the
+  // image occupies a head and a tail range along the last dimension, so the
+  // transform runs as batched (D-1)-dimensional FFTs over those slices only
+  // plus one strided 1-D pass along the last dimension (forward: slices
+  // first; backward: the 1-D pass first, then only the slices the crop reads).
+  cufftHandle fft = 0;        // D = 1: the transform; D >= 2: slices of the head range
+  cufftHandle fft_tail = 0;   // slices of the tail range (when its length differs)
+  cufftHandle fft_line = 0;   // strided 1-D pass along the last dimension
+  bool fft_ok = false, fft_tail_ok = false, fft_line_ok = false;
+  int64_t slice_head = 0, slice_tail = 0, slice_size = 0;
+  void* fft_work = nullptr;
   size_t real_size = 4;
 
   void* grid = nullptr;       // tmpVec, |Ntilde| complex
@@ -111,10 +120,13 @@ struct nfft_plan {
   void* wtab = nullptr;       // M * D * 2m (T), sorted window tensor (not for POLYNOMIAL)
   int32_t* tile_start = nullptr;   // ntiles_total + 1: CSR of nodes per home tile
   void* cbuf = nullptr;       // M complex scratch for real-valued convolve calls (lazy)
+  void* fsorted = nullptr;    // M complex: fHat in bin-sorted order (spreading input)
   // spreading tasks: (home tile, first node, end node, 0), hot tiles split
   int64_t n_tasks = 0;
   int4* tasks = nullptr;
-  int spread_pitch = 0;            // shared-memory row pitch of the padded tile
+  int spread_pitch = 0;            // shared-memory row pitch of the padded spreading tile
+  int gather_pitch = 0;            // shared-memory row pitch of the staged gather tile
+  bool gather_tiled = false;       // gather from shared-memory tiles (else straight from L1/L2)
   int* dflag = nullptr;            // device status word
   size_t scratch_bytes = 0;
 
@@ -142,6 +154,8 @@ int launch_build_node_tables(const nfft_plan* p, const int32_t* perm, const int3
 int launch_build_weight_table(const nfft_plan* p);
 int launch_deconv_factors(nfft_plan* p);
 int launch_build_tasks(nfft_plan* p, int chunk);
+// autotune.cu
+int apply_block_size(nfft_plan* p, const int64_t* bs, const void* k);
 // sort.cu
 int radix_sort_pairs(uint32_t* keys, int32_t* vals, uint32_t* keys_tmp, int32_t* vals_tmp, int64_t n,
                      int key_bits, void* scratch, size_t scratch_bytes, cudaStream_t s,

@@ -7,6 +7,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <algorithm>
+#include <cstdlib>
 #include <cstring>
 #include <vector>
 
@@ -131,9 +132,10 @@ int64_t lut_size_for(int m) {
 }
 
 void default_block(nfft_plan* p) {
-  // Tiles of about 4096 points in FP32 (32 KiB of accumulators), halved in
-  // FP64; the reference's blockSize keyword overrides them.
-  int64_t def[3][3] = {{4096, 1, 1}, {64, 64, 1}, {16, 16, 16}};
+  // Default tiles (the autotuner refines them): 16^3 (3-D), 32^2 (2-D, two
+  // warps per CTA), 4096 (1-D); the last dimension halved in FP64.  The
+  // reference's blockSize keyword overrides them.
+  int64_t def[3][3] = {{4096, 1, 1}, {32, 32, 1}, {16, 16, 16}};
   for (int d = 0; d < 3; ++d) {
     int64_t b = def[p->D - 1][d];
     if (p->precision == 64 && d == p->D - 1) b = b > 1 ? b / 2 : 1;
@@ -151,6 +153,8 @@ void free_nodes(nfft_plan* p) {
   cudaFree(p->wtab);
   cudaFree(p->tile_start);
   cudaFree(p->tasks);
+  cudaFree(p->fsorted);
+  p->fsorted = nullptr;
   p->k = p->frac4 = p->wtab = nullptr;
   p->node4 = nullptr;
   p->tile_start = nullptr;
@@ -187,13 +191,99 @@ int cufft_check(cufftResult r, const char* what) {
   return NFFT_OK;
 }
 
-int exec_fft(nfft_plan* p, int dir) {
+int exec_one(nfft_plan* p, cufftHandle h, int64_t offset, int dir) {
   if (p->precision == 32) {
-    auto* g = static_cast<cufftComplex*>(p->grid);
-    return cufft_check(cufftExecC2C(p->fft, g, g, dir), "exec");
+    auto* g = static_cast<cufftComplex*>(p->grid) + offset;
+    return cufft_check(cufftExecC2C(h, g, g, dir), "exec");
   }
-  auto* g = static_cast<cufftDoubleComplex*>(p->grid);
-  return cufft_check(cufftExecZ2Z(p->fft, g, g, dir), "exec");
+  auto* g = static_cast<cufftDoubleComplex*>(p->grid) + offset;
+  return cufft_check(cufftExecZ2Z(h, g, g, dir), "exec");
+}
+
+// FFT of the plan's grid, unnormalised, forward sign -1 / backward +1
+// (plan_fft! / plan_bfft!, src/implementation.jl:87-88).
+int exec_fft(nfft_plan* p, int dir) {
+  if (!p->fft_line_ok) return exec_one(p, p->fft, 0, dir);
+  const int64_t ntl = p->Nt[p->D - 1];
+  auto slices = [&]() -> int {
+    int rc = NFFT_OK;
+    if (p->slice_head > 0) rc = exec_one(p, p->fft, 0, dir);
+    if (!rc && p->slice_tail > 0)
+      rc = exec_one(p, p->fft_tail_ok ? p->fft_tail : p->fft, (ntl - p->slice_tail) * p->slice_size, dir);
+    return rc;
+  };
+  int rc;
+  if (dir == CUFFT_FORWARD) {
+    rc = slices();
+    if (!rc) rc = exec_one(p, p->fft_line, 0, dir);
+  } else {
+    rc = exec_one(p, p->fft_line, 0, dir);
+    if (!rc) rc = slices();
+  }
+  return rc;
+}
+
+// cuFFT plans of the grid transform with one shared work area.
+int make_fft_plans(nfft_plan* p) {
+  const cufftType type = p->precision == 32 ? CUFFT_C2C : CUFFT_Z2Z;
+  const int D = p->D;
+  size_t ws[3] = {0, 0, 0};
+  auto mk = [&](cufftHandle* h, bool* ok, int rank, int* n, int* embed, int stride, int dist, int batch,
+                size_t* w) -> int {
+    int rc = cufft_check(cufftCreate(h), "create");
+    if (rc) return rc;
+    *ok = true;
+    rc = cufft_check(cufftSetAutoAllocation(*h, 0), "auto allocation");
+    if (rc) return rc;
+    return cufft_check(cufftMakePlanMany(*h, rank, n, embed, stride, dist, embed, stride, dist, type, batch, w),
+                       "plan");
+  };
+  int rc;
+  if (D == 1) {
+    int n[1] = {int(p->Nt[0])};
+    rc = mk(&p->fft, &p->fft_ok, 1, n, nullptr, 1, 0, 1, &ws[0]);
+    if (rc) return rc;
+  } else {
+    const int64_t nl = p->N[D - 1];
+    p->slice_head = nl - nl / 2;  // image rows n >= N/2 land at 0 .. ceil(N/2)-1
+    p->slice_tail = nl / 2;       // image rows n < N/2 land at Ntilde - N/2 ..
+    p->slice_size = D == 3 ? p->Nt[0] * p->Nt[1] : p->Nt[0];
+    int n_in[2];
+    const int rank_in = D - 1;
+    if (D == 3) {
+      n_in[0] = int(p->Nt[1]);
+      n_in[1] = int(p->Nt[0]);
+    } else {
+      n_in[0] = int(p->Nt[0]);
+    }
+    rc = mk(&p->fft, &p->fft_ok, rank_in, n_in, nullptr, 1, int(p->slice_size), int(p->slice_head), &ws[0]);
+    if (rc) return rc;
+    if (p->slice_tail > 0 && p->slice_tail != p->slice_head) {
+      rc = mk(&p->fft_tail, &p->fft_tail_ok, rank_in, n_in, nullptr, 1, int(p->slice_size), int(p->slice_tail),
+              &ws[1]);
+      if (rc) return rc;
+    }
+    int n_l[1] = {int(p->Nt[D - 1])};
+    int emb[1] = {int(p->Nt[D - 1])};
+    rc = mk(&p->fft_line, &p->fft_line_ok, 1, n_l, emb, int(p->slice_size), 1, int(p->slice_size), &ws[2]);
+    if (rc) return rc;
+  }
+  const size_t wmax = std::max(ws[0], std::max(ws[1], ws[2]));
+  if (wmax > 0) {
+    if (cudaMalloc(&p->fft_work, wmax) != cudaSuccess) {
+      set_error("cudaMalloc of the cuFFT work area (%zu bytes) failed", wmax);
+      return NFFT_ERR_ALLOC;
+    }
+    p->scratch_bytes += wmax;
+  }
+  cufftHandle hs[3] = {p->fft, p->fft_tail, p->fft_line};
+  bool oks[3] = {p->fft_ok, p->fft_tail_ok, p->fft_line_ok};
+  for (int i = 0; i < 3; ++i) {
+    if (!oks[i]) continue;
+    if ((rc = cufft_check(cufftSetWorkArea(hs[i], p->fft_work), "work area"))) return rc;
+    if ((rc = cufft_check(cufftSetStream(hs[i], p->stream), "set stream"))) return rc;
+  }
+  return NFFT_OK;
 }
 
 // Harvest one ring slot (waits for its last event).
@@ -354,7 +444,11 @@ int nfft_plan_create(nfft_plan** out, int precision, int D, const int64_t* N, in
   p->sigma = double(p->Nt[0]) / double(p->N[0]);  // sigma = Ntilde/N, :30
   p->lut_size = lut_size_for(p->m);
   default_block(p);
-  p->spread_pitch = spread_pitch_for(D, p->m, int(p->bs[0]) + 2 * p->m - 1, precision == 32 ? 4 : 8);
+  p->spread_pitch = spread_pitch_for(D, p->m, int(p->bs[0]) + 2 * p->m - 1,
+                                     int((prm.compensated ? 4 : 2) * (precision == 32 ? 4 : 8)));
+  p->gather_pitch = spread_pitch_for(D == 2 ? 3 : D, p->m, int(p->bs[0]) + 2 * p->m - 1,
+                                     int(2 * (precision == 32 ? 4 : 8)));
+  if (const char* e = getenv("NFFT_GB300_GATHER_TILED")) p->gather_tiled = e[0] == '1';
   p->ntiles_total = 1;
   for (int d = 0; d < 3; ++d) {
     p->ntiles[d] = (p->Nt[d] + p->bs[d] - 1) / p->bs[d];
@@ -420,15 +514,8 @@ int nfft_plan_create(nfft_plan** out, int precision, int D, const int64_t* N, in
   }
   int rc = launch_deconv_factors(p);
   if (rc) return fail(rc);
-  // cuFFT: Julia's column-major Ntilde is C-order reversed
-  int n[3];
-  for (int d = 0; d < D; ++d) n[d] = int(p->Nt[D - 1 - d]);
-  rc = cufft_check(cufftPlanMany(&p->fft, D, n, nullptr, 1, 0, nullptr, 1, 0,
-                                 precision == 32 ? CUFFT_C2C : CUFFT_Z2Z, 1),
-                   "plan");
-  if (rc) return fail(rc);
-  p->fft_ok = true;
-  rc = cufft_check(cufftSetStream(p->fft, p->stream), "set stream");
+  // cuFFT plans (Julia's column-major grid is C order with reversed dims)
+  rc = make_fft_plans(p);
   if (rc) return fail(rc);
   if (prm.timing) {
     p->timing_on = true;
@@ -455,6 +542,9 @@ int nfft_plan_destroy(nfft_plan* p) {
   cudaFree(p->dflag);
   cudaFree(p->cbuf);
   if (p->fft_ok) cufftDestroy(p->fft);
+  if (p->fft_tail_ok) cufftDestroy(p->fft_tail);
+  if (p->fft_line_ok) cufftDestroy(p->fft_line);
+  cudaFree(p->fft_work);
   if (p->timing_on)
     for (int s = 0; s < nfft_plan::kRing; ++s)
       for (int i = 0; i < 4; ++i) cudaEventDestroy(p->ev[s][i]);
@@ -465,7 +555,10 @@ int nfft_plan_destroy(nfft_plan* p) {
 int nfft_set_stream(nfft_plan* p, void* stream) {
   if (!p) return NFFT_ERR_INVALID_ARG;
   p->stream = static_cast<cudaStream_t>(stream);
-  return cufft_check(cufftSetStream(p->fft, p->stream), "set stream");
+  int rc = cufft_check(cufftSetStream(p->fft, p->stream), "set stream");
+  if (!rc && p->fft_tail_ok) rc = cufft_check(cufftSetStream(p->fft_tail, p->stream), "set stream");
+  if (!rc && p->fft_line_ok) rc = cufft_check(cufftSetStream(p->fft_line, p->stream), "set stream");
+  return rc;
 }
 
 int nfft_set_nodes(nfft_plan* p, const void* k, int k_on_device) {
@@ -545,7 +638,11 @@ int nfft_set_nodes(nfft_plan* p, const void* k, int k_on_device) {
     // hot tiles are split into chunks of at most 1024 nodes
     rc = launch_build_tasks(p, 1024);
     if (rc) return rc;
-    p->scratch_bytes += sizeof(int4) * size_t(p->n_tasks);
+    if (cudaMalloc(&p->fsorted, 2 * rs * size_t(M > 0 ? M : 1)) != cudaSuccess) {
+      set_error("cudaMalloc of the sorted value buffer failed");
+      return NFFT_ERR_ALLOC;
+    }
+    p->scratch_bytes += sizeof(int4) * size_t(p->n_tasks) + 2 * rs * size_t(M);
   }
   NFFT_CUDA_TRY(cudaStreamSynchronize(s));
   NFFT_CUDA_TRY(cudaGetLastError());

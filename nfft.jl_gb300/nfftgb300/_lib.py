@@ -79,6 +79,8 @@ SIGNATURES = {
     "nfft_deconvolve": (_I, [_P, _P, _P]),
     "nfft_deconvolve_transpose": (_I, [_P, _P, _P]),
     "nfft_grad_nodes": (_I, [_P, _P, _P, _P]),
+    "nfft_autotune": (_I, [_P, _I]),
+    "nfft_set_block_size": (_I, [_P, _I64P]),
     "nfft_get_info": (_I, [_P, ctypes.POINTER(nfft_info)]),
     "nfft_grid": (_P, [_P]),
     "nfft_get_timing": (_I, [_P, ctypes.POINTER(ctypes.c_double)]),

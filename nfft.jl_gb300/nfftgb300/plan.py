@@ -455,6 +455,27 @@ class GB300NFFTPlan:
         _check(L.load().nfft_grad_nodes(self._handle, _ptr(v), _ptr(w), _ptr(dk)))
         return dk
 
+    def autotune(self, use_cache=True):
+        """Pick the fastest spreading tile shape for these nodes (re-bins)."""
+        self._sync_stream()
+        _check(L.load().nfft_autotune(self._handle, int(bool(use_cache))))
+        self._refresh_info()
+        return self.params.blockSize
+
+    def set_block_size(self, bs):
+        """Re-tile the plan (blockSize) and re-bin its nodes."""
+        arr = (ctypes.c_int64 * 3)(*(list(bs) + [1] * (3 - len(bs))))
+        self._sync_stream()
+        _check(L.load().nfft_set_block_size(self._handle, arr))
+        self._refresh_info()
+        return self.params.blockSize
+
+    def _refresh_info(self):
+        info = L.nfft_info()
+        _check(L.load().nfft_get_info(self._handle, ctypes.byref(info)))
+        self._info = info
+        self.params.blockSize = tuple(int(info.block_size[d]) for d in range(len(self.N)))
+
     # -------------------------------------------------------------- diagnostics
     def binning(self):
         """Integer outputs of the device binning (host numpy arrays)."""

@@ -312,3 +312,51 @@ def test_sdc_equispaced(pre):
     np.testing.assert_allclose(wn, 1 / 72, rtol=np.sqrt(np.finfo(np.float32).eps))
     op = oracle.OraclePlan(nodes, N, m=5, sigma=2.0, precompute=int(pre), dtype=np.float32)
     np.testing.assert_allclose(wn, oracle.sdc(op, iters=10), rtol=1e-5)
+
+
+def test_config5_spiral_gradients_full_size():
+    """Differentiated 2-D spiral NFFT: N = (256, 256), 32 interleaves x 2048
+    samples of an Archimedean spiral reaching |k| = 0.5, loss ||A(k) f - y||^2
+    in FP32 with gradients in f and k; the k-gradient is checked against FP64
+    central finite differences (step 1e-6) of the same loss on an FP64 plan,
+    and the f-gradient against 2 A^H (A f - y)."""
+    N = (256, 256)
+    k64 = spiral_nodes(256, 32, 2048)
+    M = k64.shape[1]
+    f = cnormal(N, 21)
+    yt = cnormal(M, 22)
+    k32 = k64.astype(np.float32)
+    p32 = nf.plan_nfft(k32, N, m=4, sigma=2.0)
+    kt = torch.tensor(k32, device="cuda", requires_grad=True)
+    fd = nf.as_colmajor(f, N, torch.complex64).requires_grad_(True)
+    ytd = torch.tensor(yt.astype(np.complex64), device="cuda")
+    loss = (autodiff.nfft_nodes(kt, fd, p32) - ytd).abs().pow(2).sum()
+    loss.backward()
+    gk = kt.grad.cpu().numpy().astype(np.float64)
+    # FP64 reference loss for finite differences (nodes as the FP32 plan saw them)
+    kref = k32.astype(np.float64)
+    q = nf.plan_nfft(kref, N, m=4, sigma=2.0)
+    f64 = nf.as_colmajor(f.astype(np.complex64).astype(np.complex128), N, torch.complex128)
+    y64 = torch.tensor(yt.astype(np.complex64).astype(np.complex128), device="cuda")
+
+    def L(kk):
+        q.nodes_(kk)
+        return float(((q * f64) - y64).abs().pow(2).sum())
+
+    rng = np.random.default_rng(5)
+    h = 1e-6
+    num, ana = [], []
+    for j in rng.choice(M, 16, replace=False):
+        for d in range(2):
+            kp, km = kref.copy(), kref.copy()
+            kp[d, j] += h
+            km[d, j] -= h
+            num.append((L(kp) - L(km)) / (2 * h))
+            ana.append(gk[d, j])
+    num, ana = np.array(num), np.array(ana)
+    assert np.linalg.norm(num - ana) / np.linalg.norm(num) < 1e-3
+    # gradient in f
+    q.nodes_(kref)
+    r = q * f64 - y64
+    ref = (2 * (nf.adjoint(q) * r)).cpu().numpy()
+    assert oracle.rel_l2(fd.grad.cpu().numpy().astype(np.complex128), ref) < 1e-4

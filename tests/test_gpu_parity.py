@@ -164,3 +164,16 @@ def test_polynomial_and_tensor_agree(pre):
     y, x = gpu_fwd_adj(p, f, fhat)
     assert oracle.rel_l2(y, op.forward(f)) < TOL64
     assert oracle.rel_l2(colmajor_flat(x), colmajor_flat(op.adjoint(fhat))) < TOL64
+
+
+@pytest.mark.parametrize("D,N", [(2, (20, 17)), (2, (33, 16)), (3, (10, 9, 7)), (3, (8, 6, 11))])
+def test_pruned_fft_odd_and_even_sizes(D, N):
+    """The grid FFT runs pruned (slices holding image data + one strided pass);
+    odd/even image sizes give head and tail slice ranges of different length."""
+    M = 3 * int(np.prod(N))
+    k, f, fhat = rand_problem(D, N, M, seed=77)
+    p = nf.plan_nfft(k, N, m=4, sigma=2.0)
+    op = oracle.OraclePlan(k, N, m=4, sigma=2.0)
+    y, x = gpu_fwd_adj(p, f, fhat)
+    assert oracle.rel_l2(y, op.forward(f)) < TOL64
+    assert oracle.rel_l2(colmajor_flat(x), colmajor_flat(op.adjoint(fhat))) < TOL64
