@@ -239,6 +239,28 @@ int nfft_get_deconv_factors(nfft_plan* plan, void* out);
 int nfft_bin_nodes_noalloc(int precision, int D, const int64_t* Ntilde, const int64_t* block_size, int64_t M,
                            const void* k, int32_t* perm, int32_t* tile_start, void* stream);
 
+/* Batched plans (no reference counterpart: NFFT.jl transforms one plan per
+ * mul! call, src/implementation.jl:145-204, and a set of plans is a loop of
+ * such calls).  A batch runs the forward (or adjoint) transforms of many
+ * plans of uneven N and M as one launch per stage over all plans -- pad,
+ * the plans' FFTs, gather (forward); value sort, spreading with tasks of all
+ * plans taken from one counter, the plans' FFTs, crop (adjoint) -- captured
+ * once per direction into a CUDA graph on `stream` and replayed.  Members
+ * need nodes, blocking = 1, compensated = 0, D = 2 or 3, and the same
+ * precision, D, m and window-evaluation mode (POLYNOMIAL or table); their
+ * grids and tile shapes may differ.  The batch uses the plans' grids and
+ * sets their stream to `stream`; a member may not be used elsewhere while
+ * the batch's call is in flight, and must outlive the batch.  After
+ * nfft_set_nodes (or a block-size change) on a member the batch refuses to
+ * run: create it again.  A NULL stream (legacy default) makes the batch use
+ * a blocking stream of its own, ordered with the legacy stream. */
+typedef struct nfft_batch nfft_batch;
+int nfft_batch_create(nfft_batch** batch, nfft_plan* const* plans, int nplans, void* stream);
+int nfft_batch_destroy(nfft_batch* batch);
+/* f[i]: image of plan i (N_i complex), fhat[i]: its M_i node values. */
+int nfft_batch_forward(nfft_batch* batch, const void* const* f, void* const* fhat);
+int nfft_batch_adjoint(nfft_batch* batch, const void* const* fhat, void* const* f);
+
 /* Wait for the plan's stream. */
 int nfft_sync(nfft_plan* plan);
 

@@ -114,6 +114,7 @@ struct nfft_plan {
   double coeffs_host[nfft::kMaxDeg * nfft::kMaxL] = {};
 
   bool has_nodes = false;
+  int64_t nodes_version = 0;  // bumped by every successful nfft_set_nodes
   void* k = nullptr;          // D x M nodes (T), user order
   int4* node4 = nullptr;      // M, sorted: trunc per dim + input index
   void* frac4 = nullptr;      // 4M (T), sorted: fractional offsets
@@ -173,6 +174,8 @@ int launch_real_part(const nfft_plan* p, const void* in, void* out, int64_t n);
 int launch_interp(const nfft_plan* p, const void* g, int g_real, void* fhat, int fhat_real);
 // spread.cu
 int launch_spread(nfft_plan* p, const void* fhat, int fhat_real, void* g, int g_real);
+// plan.cu: the grid FFT of a plan (pruned for D >= 2)
+int exec_fft_plan(nfft_plan* p, int dir);
 // gradk.cu
 int launch_grad_nodes(const nfft_plan* p, const void* g, const void* w, void* dk);
 // plain.cu (per-node kernels of the plain path, blocking = 0)

@@ -331,6 +331,9 @@ void finish_record(nfft_plan* p, int slot, int dir) {
 }
 
 }  // namespace
+
+int exec_fft_plan(nfft_plan* p, int dir) { return exec_fft(p, dir); }
+
 }  // namespace nfft
 
 using namespace nfft;
@@ -647,6 +650,7 @@ int nfft_set_nodes(nfft_plan* p, const void* k, int k_on_device) {
   NFFT_CUDA_TRY(cudaStreamSynchronize(s));
   NFFT_CUDA_TRY(cudaGetLastError());
   p->has_nodes = true;
+  p->nodes_version += 1;
   p->timing[0] = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
   return NFFT_OK;
 }

@@ -19,334 +19,10 @@
 //   * the padded tile is added to the zeroed grid with vector global atomics
 //     (red.global.add.v2), wrapping periodically; all-zero points are skipped.
 // The lock of the reference becomes the L2 atomics of the flush.
-#include "warpnode.cuh"
+#include "spread_body.cuh"
 
 namespace nfft {
 namespace {
-
-constexpr int kSpreadThreads = 256;
-constexpr int kSpreadWarps = kSpreadThreads / 32;
-constexpr int kStageNodes = 32;
-
-template <typename T> __device__ __forceinline__ void red_add2(T* g, T x, T y);
-template <> __device__ __forceinline__ void red_add2<float>(float* g, float x, float y) {
-  atomicAdd(reinterpret_cast<float2*>(g), make_float2(x, y));
-}
-template <> __device__ __forceinline__ void red_add2<double>(double* g, double x, double y) {
-  atomicAdd(g, x);
-  atomicAdd(g + 1, y);
-}
-
-// Accumulator element: (re, im) or, compensated, (re, im, comp re, comp im).
-template <typename T, bool KAHAN> struct Acc;
-template <> struct Acc<float, false> { using type = float2; };
-template <> struct Acc<double, false> { using type = double2; };
-template <> struct Acc<float, true> { using type = float4; };
-template <> struct Acc<double, true> { struct __align__(32) type { double x, y, z, w; }; };
-
-template <typename A, typename T> __device__ __forceinline__ void acc_add(A& a, T vr, T vi);
-template <> __device__ __forceinline__ void acc_add<float2, float>(float2& a, float vr, float vi) {
-  a.x += vr;
-  a.y += vi;
-}
-template <> __device__ __forceinline__ void acc_add<double2, double>(double2& a, double vr, double vi) {
-  a.x += vr;
-  a.y += vi;
-}
-template <typename A, typename T> __device__ __forceinline__ void kahan_add(A& a, T vr, T vi) {
-  // Kahan: y = v - c; t = s + y; c = (t - s) - y; s = t
-  const T yr = vr - a.z, yi = vi - a.w;
-  const T tr = a.x + yr, ti = a.y + yi;
-  a.z = (tr - a.x) - yr;
-  a.w = (ti - a.y) - yi;
-  a.x = tr;
-  a.y = ti;
-}
-
-// --------------------------------------------------------------------------
-// D >= 2: slice-owned, atomic-free.
-//
-// OwnedCfg: NW warps per CTA own the slices along the last dimension with
-// index = warp mod NW.  D = 3: NW = 8, a slice is an x-y plane of L x L taps,
-// lanes = (tap x, row slot), NSTEP steps over the rows.  D = 2: NW = 2, a
-// warp's taps of one node are ceil(L/2) rows x L columns, flattened over the
-// lanes.  Staging precomputes per node, once per CTA, the complex value times
-// the last-dimension window value of every slice (cz) and the products of the
-// other window values (wxy), so a warp's per-node work is a few shared loads
-// and its read-modify-writes.
-template <int D, int L> struct OwnedCfg {
-  static constexpr int NW = D == 3 ? 8 : 2;
-  static constexpr int THREADS = NW * 32;
-  static constexpr int KS = (L + NW - 1) / NW;              // owned slices per node (max)
-  static constexpr int XY = D == 3 ? L * L : L;              // staged products per node
-  static constexpr int RY = D == 3 ? 32 / L : 1;             // D = 3 row slots per step
-  static constexpr int NSTEP = D == 3 ? (L + RY - 1) / RY : (KS * L + 31) / 32;
-};
-
-template <int D, int L, typename T, bool TABLE, bool KAHAN>
-__global__ void __launch_bounds__(OwnedCfg<D, L>::THREADS) spread_owned_kernel(Geom<T> G, Nodes<T> Nd,
-                                                                               const int4* __restrict__ tasks,
-                                                                               const typename Cplx<T>::type* __restrict__ fsorted,
-                                                                               T* __restrict__ g, int pitch) {
-  static_assert(D >= 2, "slice ownership needs D >= 2");
-  using C = typename Cplx<T>::type;
-  using A = typename Acc<T, KAHAN>::type;
-  using CF = OwnedCfg<D, L>;
-  constexpr int DL = D * L;
-  constexpr int DEG = L + 1;
-  constexpr int NB = kStageNodes;
-  constexpr int WPT = (NB * DL + CF::THREADS - 1) / CF::THREADS;  // staged window values per thread
-  extern __shared__ __align__(32) unsigned char smem_raw[];
-  const int4 task = tasks[blockIdx.x];
-  const int tile = task.x;
-  const int tc0 = tile % G.ntiles[0];
-  const int tc1 = (tile / G.ntiles[0]) % G.ntiles[1];
-  const int tc2 = tile / (G.ntiles[0] * G.ntiles[1]);
-  const int P0 = G.bs[0] + L - 1;
-  const int P1 = G.bs[1] + L - 1;
-  const int P2 = D == 3 ? G.bs[2] + L - 1 : 1;
-  const int o0 = tc0 * G.bs[0], o1 = tc1 * G.bs[1], o2 = D == 3 ? tc2 * G.bs[2] : 0;
-  const int plane = pitch * P1;
-  const int nacc = plane * P2;
-  const int slice_stride = D == 3 ? plane : pitch;
-  A* acc = reinterpret_cast<A*>(smem_raw);
-  int2* s_meta = reinterpret_cast<int2*>(smem_raw + ((size_t(nacc) * sizeof(A) + 31) & ~size_t(31)));
-  C* s_cz = reinterpret_cast<C*>(s_meta + NB);   // [NB][L]
-  C* s_c = s_cz + NB * L;                        // [NB]
-  T* s_w = reinterpret_cast<T*>(s_c + NB);       // [NB][DL]
-  T* s_xy = s_w + NB * DL;                       // [NB][XY]
-  {
-    A zero;
-    memset(&zero, 0, sizeof(A));
-    for (int q = threadIdx.x; q < nacc; q += blockDim.x) acc[q] = zero;
-  }
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  // static per-lane tap pattern: product index and shared offset of each step
-  int xy_idx[CF::NSTEP], lofs[CF::NSTEP], kslice[CF::NSTEP];
-  bool act[CF::NSTEP];
-#pragma unroll
-  for (int st = 0; st < CF::NSTEP; ++st) {
-    if constexpr (D == 3) {
-      const int ix = lane % L, iy = st * CF::RY + lane / L;
-      act[st] = (lane / L) < CF::RY && iy < L;
-      const int iyc = act[st] ? iy : 0;
-      xy_idx[st] = iyc * L + ix;
-      lofs[st] = iyc * pitch + ix;
-      kslice[st] = 0;
-    } else {
-      const int item = lane + 32 * st;
-      const int k = item / L, ix = item % L;
-      act[st] = k < CF::KS;
-      xy_idx[st] = ix;
-      lofs[st] = ix;
-      kslice[st] = act[st] ? k : 0;
-    }
-  }
-
-  // register prefetch of one batch: node, value (bin-sorted order), window
-  // values (or fractional offsets for the polynomial)
-  int4 r_nd = make_int4(0, 0, 0, 0);
-  C r_c;
-  T r_w[WPT];
-  auto prefetch = [&](int b) {
-    const int n = min(NB, task.z - b);
-    if (threadIdx.x < n) {
-      r_nd = __ldg(Nd.node4 + b + threadIdx.x);
-      r_c = __ldg(fsorted + b + threadIdx.x);
-    }
-#pragma unroll
-    for (int u = 0; u < WPT; ++u) {
-      const int q = threadIdx.x + u * CF::THREADS;
-      if (q < n * DL) {
-        const int s = q / DL, r = q - s * DL;
-        if constexpr (TABLE) r_w[u] = __ldg(Nd.wtab + int64_t(b + s) * DL + r);
-        else r_w[u] = __ldg(Nd.frac4 + 4 * int64_t(b + s) + r / L);
-      }
-    }
-  };
-  if (task.y < task.z) prefetch(task.y);
-  __syncthreads();
-
-  for (int b = task.y; b < task.z; b += NB) {
-    const int n = min(NB, task.z - b);
-    // stage 1: registers -> shared (window values evaluated here for POLYNOMIAL)
-    if (threadIdx.x < n) {
-      const int px = r_nd.x - o0, py = r_nd.y - o1;
-      s_meta[threadIdx.x] = D == 3 ? make_int2(r_nd.z - o2, py * pitch + px) : make_int2(py, px);
-      s_c[threadIdx.x] = r_c;
-    }
-#pragma unroll
-    for (int u = 0; u < WPT; ++u) {
-      const int q = threadIdx.x + u * CF::THREADS;
-      if (q < n * DL) {
-        T w = r_w[u];
-        if constexpr (!TABLE) {
-          const int l = (q % DL) % L;
-          const T t = w - T(0.5);
-          const T* c = G.coeffs + l * DEG;
-          w = __ldg(c + DEG - 1);
-#pragma unroll
-          for (int i = DEG - 2; i >= 0; --i) w = fma(w, t, __ldg(c + i));
-        }
-        s_w[q] = w;
-      }
-    }
-    __syncthreads();
-    // stage 2: per-slice values and tap products
-    for (int q = threadIdx.x; q < n * (L + CF::XY); q += blockDim.x) {
-      const int s = q / (L + CF::XY), r = q - s * (L + CF::XY);
-      if (r < L) {
-        const T wl = s_w[s * DL + (D - 1) * L + r];
-        const C c = s_c[s];
-        C v;
-        v.x = c.x * wl;
-        v.y = c.y * wl;
-        s_cz[s * L + r] = v;
-      } else {
-        const int u = r - L;
-        if constexpr (D == 3) {
-          const int iy = u / L, jx = u - iy * L;
-          s_xy[s * CF::XY + u] = s_w[s * DL + jx] * s_w[s * DL + L + iy];
-        } else {
-          s_xy[s * CF::XY + u] = s_w[s * DL + u];
-        }
-      }
-    }
-    __syncthreads();
-    // the next batch's global loads overlap the spreading of this one
-    if (b + NB < task.z) prefetch(b + NB);
-    for (int s = 0; s < n; ++s) {
-      const int2 meta = s_meta[s];
-      const int plast = meta.x;
-      const int is0 = (warp - plast) & (CF::NW - 1);
-      if constexpr (D == 3) {
-#pragma unroll
-        for (int k = 0; k < CF::KS; ++k) {
-          const int is = is0 + k * CF::NW;
-          if (is < L) {
-            const C cz = s_cz[s * L + is];
-            const int so = (plast + is) * slice_stride + meta.y;
-#pragma unroll
-            for (int st = 0; st < CF::NSTEP; ++st) {
-              if (act[st]) {
-                const T w = s_xy[s * CF::XY + xy_idx[st]];
-                A& a = acc[so + lofs[st]];
-                if constexpr (KAHAN) kahan_add<A, T>(a, cz.x * w, cz.y * w);
-                else acc_add<A, T>(a, cz.x * w, cz.y * w);
-              }
-            }
-          }
-        }
-      } else {
-#pragma unroll
-        for (int st = 0; st < CF::NSTEP; ++st) {
-          const int is = is0 + kslice[st] * CF::NW;
-          if (act[st] && is < L) {
-            const C cz = s_cz[s * L + is];
-            const T w = s_xy[s * CF::XY + xy_idx[st]];
-            A& a = acc[(plast + is) * slice_stride + meta.y + lofs[st]];
-            if constexpr (KAHAN) kahan_add<A, T>(a, cz.x * w, cz.y * w);
-            else acc_add<A, T>(a, cz.x * w, cz.y * w);
-          }
-        }
-      }
-    }
-    __syncthreads();
-  }
-
-  // flush: padded point (x, y, z) -> grid ((o - m + 1 + x) mod Ntilde, ...)
-  const int m1 = G.m - 1;
-  const bool small = G.small_grid;
-  const int rows = P1 * P2;
-  for (int r = warp; r < rows; r += CF::NW) {
-    const int y = r % P1, z = r / P1;
-    const int gy = small ? wrap_any(o1 - m1 + y, G.Nt[1]) : wrap_once(o1 - m1 + y, G.Nt[1]);
-    const int gz = D == 3 ? (small ? wrap_any(o2 - m1 + z, G.Nt[2]) : wrap_once(o2 - m1 + z, G.Nt[2])) : 0;
-    T* grow = g + 2 * (int64_t(gz) * G.plane + int64_t(gy) * G.Nt[0]);
-    const A* srow = acc + z * plane + y * pitch;
-    for (int x = lane; x < P0; x += 32) {
-      const A a = srow[x];
-      T vr = a.x, vi = a.y;
-      if constexpr (KAHAN) {
-        vr -= a.z;
-        vi -= a.w;
-      }
-      if (vr != T(0) || vi != T(0)) {
-        const int gx = small ? wrap_any(o0 - m1 + x, G.Nt[0]) : wrap_once(o0 - m1 + x, G.Nt[0]);
-        red_add2<T>(grow + 2 * gx, vr, vi);
-      }
-    }
-  }
-}
-
-// --------------------------------------------------------------------------
-// D = 1: 32/G nodes per warp, shared-memory atomics into the padded row.
-template <int L, typename T, bool TABLE>
-__global__ void __launch_bounds__(kSpreadThreads) spread_pad1_kernel(Geom<T> G, Nodes<T> Nd,
-                                                                      const int4* __restrict__ tasks,
-                                                                      const typename Cplx<T>::type* __restrict__ fhat,
-                                                                      T* __restrict__ g) {
-  using C = typename Cplx<T>::type;
-  using LN = Lanes<1, L>;
-  extern __shared__ __align__(32) unsigned char smem_raw[];
-  const int4 task = tasks[blockIdx.x];
-  const int o0 = task.x * G.bs[0];
-  const int P0 = G.bs[0] + L - 1;
-  T* sre = reinterpret_cast<T*>(smem_raw);
-  T* sim = sre + P0;
-  for (int q = threadIdx.x; q < P0; q += blockDim.x) {
-    sre[q] = T(0);
-    sim[q] = T(0);
-  }
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int slot = lane / LN::G1, ix = lane % LN::G1;
-  const bool act = ix < L;
-  T c[LN::DEG];
-  if constexpr (!TABLE) {
-#pragma unroll
-    for (int q = 0; q < LN::DEG; ++q) c[q] = act ? __ldg(G.coeffs + ix * LN::DEG + q) : T(0);
-  }
-  __syncthreads();
-  for (int b = task.y + warp * LN::NPW; b < task.z; b += kSpreadWarps * LN::NPW) {
-    const int i = b + slot;
-    if (i < task.z && act) {
-      const int4 nd = __ldg(Nd.node4 + i);
-      T w;
-      if constexpr (TABLE) {
-        w = __ldg(Nd.wtab + int64_t(i) * L + ix);
-      } else {
-        const T t = __ldg(Nd.frac4 + 4 * int64_t(i)) - T(0.5);
-        w = c[LN::DEG - 1];
-#pragma unroll
-        for (int q = LN::DEG - 2; q >= 0; --q) w = fma(w, t, c[q]);
-      }
-      const C v = __ldg(fhat + nd.w);
-      const int px = nd.x - o0 + ix;
-      atomicAdd(sre + px, w * v.x);
-      atomicAdd(sim + px, w * v.y);
-    }
-  }
-  __syncthreads();
-  const int m1 = G.m - 1;
-  const bool small = G.small_grid;
-  for (int x = threadIdx.x; x < P0; x += blockDim.x) {
-    const T a = sre[x], bb = sim[x];
-    if (a != T(0) || bb != T(0)) {
-      const int gx = small ? wrap_any(o0 - m1 + x, G.Nt[0]) : wrap_once(o0 - m1 + x, G.Nt[0]);
-      red_add2<T>(g + 2 * int64_t(gx), a, bb);
-    }
-  }
-}
-
-template <int D, int L, typename T>
-size_t owned_smem(const nfft_plan* p, bool kahan) {
-  const int P1 = int(p->bs[1]) + L - 1;
-  const int P2 = D == 3 ? int(p->bs[2]) + L - 1 : 1;
-  const size_t acc = ((kahan ? 4 : 2) * sizeof(T) * size_t(p->spread_pitch) * P1 * P2 + 31) & ~size_t(31);
-  const size_t stage = kStageNodes * (sizeof(int2) + 2 * sizeof(T) * (L + 1) +
-                                      sizeof(T) * (D * L + OwnedCfg<D, L>::XY));
-  return acc + stage;
-}
 
 // fHat in bin-sorted order (node4[i].w = input index), for coalesced staging.
 template <typename T>

@@ -90,6 +90,10 @@ SIGNATURES = {
     "nfft_get_deconv_factors": (_I, [_P, _P]),
     "nfft_sync": (_I, [_P]),
     "nfft_bin_nodes_noalloc": (_I, [_I, _I, _I64P, _I64P, _I64, _P, _P, _P, _P]),
+    "nfft_batch_create": (_I, [_P, _P, _I, _P]),
+    "nfft_batch_destroy": (_I, [_P]),
+    "nfft_batch_forward": (_I, [_P, _P, _P]),
+    "nfft_batch_adjoint": (_I, [_P, _P, _P]),
     "nfft_kernel_launch_count": (_I64, []),
     "nfft_status_string": (ctypes.c_char_p, [_I]),
     "nfft_last_error": (ctypes.c_char_p, []),

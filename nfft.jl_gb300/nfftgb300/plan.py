@@ -612,3 +612,90 @@ def nfft_adjoint(k, N, fHat, **kw):
 
 def kernel_launch_count():
     return int(L.load().nfft_kernel_launch_count())
+
+
+class NFFTBatch:
+    """Many plans transformed together (nfft_batch_* of include/nfft_gb300.h).
+
+    No reference counterpart: NFFT.jl runs one plan per ``mul!``.  Members
+    need nodes, ``blocking=True``, ``compensated=False``, D = 2 or 3 and the
+    same precision, D, ``m`` and window-evaluation mode; each stage runs as
+    one launch over all plans, the whole direction replayed as a CUDA graph.
+    The batch runs on the stream current at creation; calls must be made
+    with that stream current.  After ``nodes_`` on a member, build the batch
+    again.
+    """
+
+    def __init__(self, plans):
+        plans = list(plans)
+        if not plans:
+            raise ArgumentError("need at least one plan")
+        dev = plans[0].device
+        if any(p.device != dev for p in plans):
+            raise ArgumentError("plans of a batch must live on one device")
+        self.plans = plans
+        self.device = dev
+        lib = L.load()
+        arr = (ctypes.c_void_p * len(plans))(*[p._handle.value for p in plans])
+        h = ctypes.c_void_p()
+        with torch.cuda.device(dev):
+            self._stream = torch.cuda.current_stream(dev).cuda_stream
+            _check(lib.nfft_batch_create(ctypes.byref(h), arr, len(plans), ctypes.c_void_p(self._stream)))
+        self._handle = h
+        for p in plans:
+            p._stream = None  # the batch re-bound the plan's stream; the next plan call re-binds it
+        self._keep = plans
+
+    def __del__(self):
+        h = getattr(self, "_handle", None)
+        if h is not None and h.value:
+            try:
+                L.load().nfft_batch_destroy(h)
+            except Exception:
+                pass
+            self._handle = None
+
+    def __len__(self):
+        return len(self.plans)
+
+    def _call(self, fn, ins, outs):
+        if len(ins) != len(self.plans) or len(outs) != len(self.plans):
+            raise DimensionMismatch(f"need {len(self.plans)} inputs and outputs")
+        if torch.cuda.current_stream(self.device).cuda_stream != self._stream:
+            raise ArgumentError("call the batch with the stream current at its creation")
+        n = len(self.plans)
+        a = (ctypes.c_void_p * n)(*[t.data_ptr() for t in ins])
+        b = (ctypes.c_void_p * n)(*[t.data_ptr() for t in outs])
+        _check(fn(self._handle, a, b))
+
+    def _lengths(self, *lists):
+        for x in lists:
+            if len(x) != len(self.plans):
+                raise DimensionMismatch(f"need {len(self.plans)} inputs and outputs, got {len(x)}")
+
+    def forward_(self, fHats, fs):
+        """mul!(fHats[i], plans[i], fs[i]) for every i."""
+        self._lengths(fHats, fs)
+        fs = [p._image(f) for p, f in zip(self.plans, fs)]
+        fHats = [p._nodevec(v) for p, v in zip(self.plans, fHats)]
+        self._call(L.load().nfft_batch_forward, fs, fHats)
+        return fHats
+
+    def adjoint_(self, fs, fHats):
+        """mul!(fs[i], adjoint(plans[i]), fHats[i]) for every i."""
+        self._lengths(fHats, fs)
+        fs = [p._image(f) for p, f in zip(self.plans, fs)]
+        fHats = [p._nodevec(v) for p, v in zip(self.plans, fHats)]
+        self._call(L.load().nfft_batch_adjoint, fHats, fs)
+        return fs
+
+    def forward(self, fs):
+        self._lengths(fs)
+        outs = [torch.empty(p.NOut, dtype=p.cdtype, device=p.device) for p in self.plans]
+        return self.forward_(outs, [as_colmajor(f, p.N, p.cdtype, p.device) for p, f in zip(self.plans, fs)])
+
+    def adjoint(self, fHats):
+        self._lengths(fHats)
+        outs = [empty_image(p.N, p.cdtype, p.device) for p in self.plans]
+        return self.adjoint_(outs, [v.to(device=p.device, dtype=p.cdtype).contiguous()
+                                    for p, v in zip(self.plans, fHats)])
