@@ -425,7 +425,16 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-check", action="store_true")
+    ap.add_argument("--small", action="store_true",
+                    help="profiling case of the same kernels: N=128^3, 2048 spokes x 256 samples (same node "
+                         "density; 134 MB grid, above L2) -- not a bench line")
     args = ap.parse_args()
+    if args.small:
+        global N3, SPOKES, SAMPLES, M_NODES, WORKLOAD
+        N3, SPOKES, SAMPLES = (128, 128, 128), 2048, 256
+        M_NODES = SPOKES * SAMPLES
+        WORKLOAD = ("3D radial koosh-ball NFFT fwd+adj, N=128^3, 2048 spokes x 256 samples (M=524288), "
+                    "KB m=4 sigma=2 (profiling case)")
     if args.impl == "reference":
         return run_reference(args)
     return run_ours(args)

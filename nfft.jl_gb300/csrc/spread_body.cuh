@@ -29,6 +29,79 @@ template <> struct Acc<double, false> { using type = double2; };
 template <> struct Acc<float, true> { using type = float4; };
 template <> struct Acc<double, true> { struct __align__(32) type { double x, y, z, w; }; };
 
+// (re, im) of an accumulator element (compensated: sum minus compensation).
+template <typename T, typename A, bool KAHAN>
+__device__ __forceinline__ void acc_value(const A& a, T& vr, T& vi) {
+  vr = a.x;
+  vi = a.y;
+  if constexpr (KAHAN) {
+    vr -= a.z;
+    vi -= a.w;
+  }
+}
+
+// Add the padded tile to the grid: padded point (x, y, z) -> grid point
+// ((o - m + 1 + x) mod Ntilde, ...); all-zero units are skipped.  FP32 on a
+// 16-byte aligned grid adds two neighbouring points per vector atomic
+// (red.global.add.v4.f32): units are grid-aligned pairs (even grid x,
+// Ntilde[0] even, so a pair never straddles the periodic wrap), and the
+// padded columns outside [0, P0) read as zero.  Otherwise (FP64, or a
+// caller's grid that is only 8-byte aligned) a unit is one point.  Lanes
+// cover (row, unit) jointly so short rows do not leave most of a warp idle.
+template <int D, typename T, bool KAHAN, int NWARPS>
+__device__ __forceinline__ void flush_tile(const Geom<T>& G, const typename Acc<T, KAHAN>::type* __restrict__ acc,
+                                           T* __restrict__ g, int o0, int o1, int o2, int P0, int P1, int P2,
+                                           int pitch) {
+  const bool pair = sizeof(T) == 4 && (reinterpret_cast<uintptr_t>(g) & 15) == 0;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int m1 = G.m - 1;
+  const bool small = G.small_grid;
+  const int Nt0 = G.Nt[0];
+  const int x0 = o0 - m1;                                  // grid x of padded column 0
+  const int lead = pair ? (x0 & 1) : 0;                    // column 0 is the odd half of a pair
+  const int nunit = pair ? (P0 + lead + 1) >> 1 : P0;      // units per row
+  const int lpr = nunit < 32 ? nunit : 32;                 // lanes per row
+  const int rpi = 32 / lpr;                                // rows per warp and iteration
+  const int rr = lane / lpr, j0 = lane - rr * lpr;
+  const int rows = P1 * P2;
+  const int plane = pitch * P1;
+  const int step = NWARPS * rpi;
+  int r = rr < rpi ? warp * rpi + rr : rows;
+  int y = r % P1, z = r / P1;
+  for (; r < rows; r += step) {
+    const int gy = small ? wrap_any(o1 - m1 + y, G.Nt[1]) : wrap_once(o1 - m1 + y, G.Nt[1]);
+    const int gz = D == 3 ? (small ? wrap_any(o2 - m1 + z, G.Nt[2]) : wrap_once(o2 - m1 + z, G.Nt[2])) : 0;
+    T* grow = g + 2 * (int64_t(gz) * G.plane + int64_t(gy) * Nt0);
+    const auto* srow = acc + z * plane + y * pitch;
+    for (int j = j0; j < nunit; j += lpr) {
+      if constexpr (sizeof(T) == 4) {
+        if (pair) {
+          const int xa = 2 * j - lead;
+          T ar = T(0), ai = T(0), br = T(0), bi = T(0);
+          if (xa >= 0) acc_value<T, typename Acc<T, KAHAN>::type, KAHAN>(srow[xa], ar, ai);
+          if (xa + 1 < P0) acc_value<T, typename Acc<T, KAHAN>::type, KAHAN>(srow[xa + 1], br, bi);
+          if (ar != T(0) || ai != T(0) || br != T(0) || bi != T(0)) {
+            const int gx = small ? wrap_any(x0 + xa, Nt0) : wrap_once(x0 + xa, Nt0);
+            atomicAdd(reinterpret_cast<float4*>(grow + 2 * gx), make_float4(ar, ai, br, bi));
+          }
+          continue;
+        }
+      }
+      T vr, vi;
+      acc_value<T, typename Acc<T, KAHAN>::type, KAHAN>(srow[j], vr, vi);
+      if (vr != T(0) || vi != T(0)) {
+        const int gx = small ? wrap_any(x0 + j, Nt0) : wrap_once(x0 + j, Nt0);
+        red_add2<T>(grow + 2 * gx, vr, vi);
+      }
+    }
+    y += step;
+    while (y >= P1) {
+      y -= P1;
+      ++z;
+    }
+  }
+}
+
 template <typename A, typename T> __device__ __forceinline__ void acc_add(A& a, T vr, T vi);
 template <> __device__ __forceinline__ void acc_add<float2, float>(float2& a, float vr, float vi) {
   a.x += vr;
@@ -237,29 +310,8 @@ __device__ __forceinline__ void spread_owned_body(const Geom<T>& G, const Nodes<
     __syncthreads();
   }
 
-  // flush: padded point (x, y, z) -> grid ((o - m + 1 + x) mod Ntilde, ...)
-  const int m1 = G.m - 1;
-  const bool small = G.small_grid;
-  const int rows = P1 * P2;
-  for (int r = warp; r < rows; r += CF::NW) {
-    const int y = r % P1, z = r / P1;
-    const int gy = small ? wrap_any(o1 - m1 + y, G.Nt[1]) : wrap_once(o1 - m1 + y, G.Nt[1]);
-    const int gz = D == 3 ? (small ? wrap_any(o2 - m1 + z, G.Nt[2]) : wrap_once(o2 - m1 + z, G.Nt[2])) : 0;
-    T* grow = g + 2 * (int64_t(gz) * G.plane + int64_t(gy) * G.Nt[0]);
-    const A* srow = acc + z * plane + y * pitch;
-    for (int x = lane; x < P0; x += 32) {
-      const A a = srow[x];
-      T vr = a.x, vi = a.y;
-      if constexpr (KAHAN) {
-        vr -= a.z;
-        vi -= a.w;
-      }
-      if (vr != T(0) || vi != T(0)) {
-        const int gx = small ? wrap_any(o0 - m1 + x, G.Nt[0]) : wrap_once(o0 - m1 + x, G.Nt[0]);
-        red_add2<T>(grow + 2 * gx, vr, vi);
-      }
-    }
-  }
+  // (the batch loop ends with a barrier: the tile is complete)
+  flush_tile<D, T, KAHAN, CF::NW>(G, acc, g, o0, o1, o2, P0, P1, P2, pitch);
 }
 
 template <int D, int L, typename T, bool TABLE, bool KAHAN>
