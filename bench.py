@@ -412,6 +412,76 @@ def run_ours(args):
     return 0
 
 
+def batched_plans(seed=4, nplans=64):
+    """64 2-D FP32 plans: N_i from {64, 96, 128, 192, 256, 384, 512} (grids of
+    2 N_i, radix-3 sizes included), M_i = floor(10^U(4, 6)), nodes U[-1/2, 1/2)^2."""
+    rng = np.random.default_rng(seed)
+    sizes = [64, 96, 128, 192, 256, 384, 512]
+    out = []
+    for _ in range(nplans):
+        n = int(rng.choice(sizes))
+        M = int(10 ** rng.uniform(4, 6))
+        out.append(((rng.random((2, M)) - 0.5).astype(np.float32), (n, n)))
+    return out
+
+
+def run_batched(args):
+    """--workload batched2d: the 64 batched 2-D plans, one graph-replayed
+    batch call per direction against a loop of single-plan calls."""
+    import torch
+    import nfftgb300 as nf
+    dev = torch.device("cuda", torch.cuda.current_device())
+    probs = batched_plans()
+    plans = [nf.plan_nfft(k, N, m=4, sigma=2.0, precompute=nf.TENSOR) for k, N in probs]
+    if args.autotune:
+        for p in plans:
+            p.autotune(use_cache=True)
+    batch = nf.NFFTBatch(plans)
+    rng = np.random.default_rng(5)
+    fs = [nf.as_colmajor(complex_normal(rng, N), N, torch.complex64, dev) for _, N in probs]
+    vs = [torch.from_numpy(complex_normal(rng, k.shape[1])).to(dev) for k, _ in probs]
+    ys = [torch.empty(k.shape[1], dtype=torch.complex64, device=dev) for k, _ in probs]
+    xs = [nf.empty_image(N, torch.complex64, dev) for _, N in probs]
+    total_m = sum(k.shape[1] for k, _ in probs)
+
+    def step_batch():
+        batch.forward_(ys, fs)
+        batch.adjoint_(xs, vs)
+
+    def step_loop():
+        for p, y, f in zip(plans, ys, fs):
+            p.forward_(y, f)
+        for p, x, v in zip(plans, xs, vs):
+            p.adjoint_(x, v)
+
+    out = {}
+    stream = torch.cuda.current_stream(dev)
+    for name, step in (("batch", step_batch), ("loop", step_loop)):
+        for _ in range(args.warmup):
+            step()
+        torch.cuda.synchronize()
+        l0 = nf.kernel_launch_count()
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ev0.record(stream)
+        for _ in range(args.steps):
+            step()
+        ev1.record(stream)
+        torch.cuda.synchronize()
+        t = ev0.elapsed_time(ev1) * 1e-3
+        out[name] = {"value": total_m * args.steps / t, "ms_per_step": t / args.steps * 1e3,
+                     "host_launch_calls": nf.kernel_launch_count() - l0}
+    print(json.dumps({
+        "metric": "batched 2-D fwd+adj NFFT nodes/s (64 plans, FP32)", "value": out["batch"]["value"],
+        "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": out["batch"]["ms_per_step"], "higher_is_better": True, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "64 plans, N_i in {64..512}^2, M_i = floor(10^U(4,6)), KB m=4 sigma=2, TENSOR",
+                   "total_nodes": total_m, "grid_sizes": sorted({2 * N[0] for _, N in probs})},
+        "loop_of_single_plans": out["loop"],
+        "note": "batch launches are captured once per direction into a CUDA graph; host_launch_calls counts "
+                "launches issued from the host (0 for graph replays)"}))
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -428,7 +498,11 @@ def main():
     ap.add_argument("--small", action="store_true",
                     help="profiling case of the same kernels: N=128^3, 2048 spokes x 256 samples (same node "
                          "density; 134 MB grid, above L2) -- not a bench line")
+    ap.add_argument("--workload", default="radial3d", choices=["radial3d", "batched2d"],
+                    help="radial3d: the headline line; batched2d: the 64 batched 2-D plans (extra measurement)")
     args = ap.parse_args()
+    if args.workload == "batched2d":
+        return run_batched(args)
     if args.small:
         global N3, SPOKES, SAMPLES, M_NODES, WORKLOAD
         N3, SPOKES, SAMPLES = (128, 128, 128), 2048, 256

@@ -28,6 +28,13 @@ struct nfft_batch {
   bool table = false;
   cudaStream_t stream = nullptr;
   cudaStream_t own_stream = nullptr;  // made when the caller passes the legacy default stream
+  // the plans' FFTs are independent: inside the captured graph they run on
+  // kSide forked streams (plan i on side[i % kSide]) and join before the
+  // next stage, so small transforms overlap instead of running back to back
+  static constexpr int kSide = 8;
+  cudaStream_t side[kSide] = {};
+  cudaEvent_t fork_ev = nullptr;
+  cudaEvent_t join_ev[kSide] = {};
   void* d_items = nullptr;        // BatchItem<T>[n]
   int64_t* d_base = nullptr;      // 5 prefix arrays of n+1: pairs, nodes, tasks, image, grid
   void** d_ptrs = nullptr;        // per call: input/output pointer of each plan
@@ -213,6 +220,29 @@ int grid_for_items(int64_t work, int per_block) {
   return int(b < 1 ? 1 : b);
 }
 
+// All plans' grid FFTs, forked over the side streams and joined back into
+// the batch stream (only ever called while the batch stream is captured).
+int forked_ffts(nfft_batch* B, int dir) {
+  const int ns = std::min(B->n, nfft_batch::kSide);
+  NFFT_CUDA_TRY(cudaEventRecord(B->fork_ev, B->stream));
+  for (int s = 0; s < ns; ++s) NFFT_CUDA_TRY(cudaStreamWaitEvent(B->side[s], B->fork_ev, 0));
+  int rc = NFFT_OK;
+  for (int i = 0; i < B->n && !rc; ++i) {
+    nfft_plan* p = B->plans[i];
+    rc = nfft_set_stream(p, B->side[i % ns]);
+    if (!rc) rc = exec_fft_plan(p, dir);
+  }
+  for (int s = 0; s < ns; ++s) {
+    NFFT_CUDA_TRY(cudaEventRecord(B->join_ev[s], B->side[s]));
+    NFFT_CUDA_TRY(cudaStreamWaitEvent(B->stream, B->join_ev[s], 0));
+  }
+  for (nfft_plan* p : B->plans) {
+    const int r2 = nfft_set_stream(p, B->stream);
+    if (!rc) rc = r2;
+  }
+  return rc;
+}
+
 template <int D, int L, typename T, bool TABLE> struct Launch {
   static int forward(nfft_batch* B) {
     const auto* items = static_cast<const BatchItem<T>*>(B->d_items);
@@ -220,10 +250,8 @@ template <int D, int L, typename T, bool TABLE> struct Launch {
     batch_pad_kernel<T><<<grid_for_items(B->total[B_PAIRS], 256), 256, 0, B->stream>>>(
         items, base + B_PAIRS * (B->n + 1), B->n, B->total[B_PAIRS], B->d_ptrs);
     NFFT_LAUNCH_CHECK();
-    for (nfft_plan* p : B->plans) {
-      int rc = exec_fft_plan(p, CUFFT_FORWARD);
-      if (rc) return rc;
-    }
+    int rc = forked_ffts(B, CUFFT_FORWARD);
+    if (rc) return rc;
     batch_gather_kernel<D, L, T, TABLE><<<B->gather_ctas, 256, 0, B->stream>>>(
         items, base + B_NODES * (B->n + 1), B->n, B->total[B_NODES], B->d_ptrs);
     NFFT_LAUNCH_CHECK();
@@ -242,10 +270,8 @@ template <int D, int L, typename T, bool TABLE> struct Launch {
     batch_spread_kernel<D, L, T, TABLE><<<B->spread_ctas, OwnedCfg<D, L>::THREADS, B->spread_smem, B->stream>>>(
         items, base + B_TASKS * (B->n + 1), B->n, B->total[B_TASKS], B->d_counter);
     NFFT_LAUNCH_CHECK();
-    for (nfft_plan* p : B->plans) {
-      int rc = exec_fft_plan(p, CUFFT_INVERSE);
-      if (rc) return rc;
-    }
+    int rc = forked_ffts(B, CUFFT_INVERSE);
+    if (rc) return rc;
     batch_crop_kernel<T><<<grid_for_items(B->total[B_IMAGE], 256), 256, 0, B->stream>>>(
         items, base + B_IMAGE * (B->n + 1), B->n, B->total[B_IMAGE], B->d_ptrs);
     NFFT_LAUNCH_CHECK();
@@ -338,6 +364,11 @@ extern "C" int nfft_batch_destroy(nfft_batch* B) {
   for (int i = 0; i < nfft_batch::kSlots; ++i)
     if (B->ring_ev[i]) cudaEventDestroy(B->ring_ev[i]);
   cudaFreeHost(B->h_ring);
+  for (int s = 0; s < nfft_batch::kSide; ++s) {
+    if (B->side[s]) cudaStreamDestroy(B->side[s]);
+    if (B->join_ev[s]) cudaEventDestroy(B->join_ev[s]);
+  }
+  if (B->fork_ev) cudaEventDestroy(B->fork_ev);
   if (B->own_stream) cudaStreamDestroy(B->own_stream);
   delete B;
   return NFFT_OK;
@@ -395,6 +426,13 @@ extern "C" int nfft_batch_create(nfft_batch** out, nfft_plan* const* plans, int 
   for (int i = 0; !rc && i < nfft_batch::kSlots; ++i)
     if (cudaEventCreateWithFlags(&B->ring_ev[i], cudaEventDisableTiming) != cudaSuccess) {
       set_error("cudaEventCreate failed");
+      rc = NFFT_ERR_CUDA;
+    }
+  if (!rc && cudaEventCreateWithFlags(&B->fork_ev, cudaEventDisableTiming) != cudaSuccess) rc = NFFT_ERR_CUDA;
+  for (int s = 0; !rc && s < nfft_batch::kSide; ++s)
+    if (cudaStreamCreateWithFlags(&B->side[s], cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&B->join_ev[s], cudaEventDisableTiming) != cudaSuccess) {
+      set_error("side stream creation failed");
       rc = NFFT_ERR_CUDA;
     }
   if (!rc) rc = run(B, 0);

@@ -271,40 +271,91 @@ __device__ __forceinline__ void spread_owned_body(const Geom<T>& G, const Nodes<
     __syncthreads();
     // the next batch's global loads overlap the spreading of this one
     if (b + NB < task.z) prefetch(b + NB);
-    for (int s = 0; s < n; ++s) {
-      const int2 meta = s_meta[s];
-      const int plast = meta.x;
-      const int is0 = (warp - plast) & (CF::NW - 1);
-      if constexpr (D == 3) {
+    // Node s+1's slice offset and values are loaded while node s's taps run
+    // (software pipeline), and all of a node's accumulator loads are issued
+    // before its stores: one node's taps hit distinct points of the slices.
+    const T* xy = s_xy;
+    if constexpr (D == 3) {
+      int so_c;
+      C cz_c[CF::KS];
+      bool ok_c[CF::KS];
+      auto load_node = [&](int s, int& so, C(&cz)[CF::KS], bool(&ok)[CF::KS]) {
+        const int2 meta = s_meta[s];
+        const int is0 = (warp - meta.x) & (CF::NW - 1);
+        so = (meta.x + is0) * slice_stride + meta.y;
 #pragma unroll
         for (int k = 0; k < CF::KS; ++k) {
           const int is = is0 + k * CF::NW;
-          if (is < L) {
-            const C cz = s_cz[s * L + is];
-            const int so = (plast + is) * slice_stride + meta.y;
+          ok[k] = is < L;
+          cz[k] = s_cz[s * L + (ok[k] ? is : 0)];
+        }
+      };
+      load_node(0, so_c, cz_c, ok_c);
+      for (int s = 0; s < n; ++s, xy += CF::XY) {
+        int so_n;
+        C cz_n[CF::KS];
+        bool ok_n[CF::KS];
+        load_node(s + 1 < n ? s + 1 : s, so_n, cz_n, ok_n);
+#pragma unroll
+        for (int k = 0; k < CF::KS; ++k) {
+          if (ok_c[k]) {
+            const int so = so_c + k * CF::NW * slice_stride;
+            A a[CF::NSTEP];
+            T w[CF::NSTEP];
 #pragma unroll
             for (int st = 0; st < CF::NSTEP; ++st) {
               if (act[st]) {
-                const T w = s_xy[s * CF::XY + xy_idx[st]];
-                A& a = acc[so + lofs[st]];
-                if constexpr (KAHAN) kahan_add<A, T>(a, cz.x * w, cz.y * w);
-                else acc_add<A, T>(a, cz.x * w, cz.y * w);
+                a[st] = acc[so + lofs[st]];
+                w[st] = xy[xy_idx[st]];
+              }
+            }
+#pragma unroll
+            for (int st = 0; st < CF::NSTEP; ++st) {
+              if (act[st]) {
+                if constexpr (KAHAN) kahan_add<A, T>(a[st], cz_c[k].x * w[st], cz_c[k].y * w[st]);
+                else acc_add<A, T>(a[st], cz_c[k].x * w[st], cz_c[k].y * w[st]);
+                acc[so + lofs[st]] = a[st];
               }
             }
           }
         }
-      } else {
+        so_c = so_n;
+#pragma unroll
+        for (int k = 0; k < CF::KS; ++k) {
+          cz_c[k] = cz_n[k];
+          ok_c[k] = ok_n[k];
+        }
+      }
+    } else {
+      int2 meta_c = s_meta[0];
+      for (int s = 0; s < n; ++s, xy += CF::XY) {
+        const int2 meta_n = s_meta[s + 1 < n ? s + 1 : s];
+        const int is0 = (warp - meta_c.x) & (CF::NW - 1);
+        A a[CF::NSTEP];
+        T w[CF::NSTEP];
+        C cz[CF::NSTEP];
+        int off[CF::NSTEP];
+        bool ok[CF::NSTEP];
 #pragma unroll
         for (int st = 0; st < CF::NSTEP; ++st) {
           const int is = is0 + kslice[st] * CF::NW;
-          if (act[st] && is < L) {
-            const C cz = s_cz[s * L + is];
-            const T w = s_xy[s * CF::XY + xy_idx[st]];
-            A& a = acc[(plast + is) * slice_stride + meta.y + lofs[st]];
-            if constexpr (KAHAN) kahan_add<A, T>(a, cz.x * w, cz.y * w);
-            else acc_add<A, T>(a, cz.x * w, cz.y * w);
+          ok[st] = act[st] && is < L;
+          if (ok[st]) {
+            off[st] = (meta_c.x + is) * slice_stride + meta_c.y + lofs[st];
+            a[st] = acc[off[st]];
+            w[st] = xy[xy_idx[st]];
+            cz[st] = s_cz[s * L + is];
           }
         }
+#pragma unroll
+        for (int st = 0; st < CF::NSTEP; ++st) {
+          if (ok[st]) {
+            if constexpr (KAHAN) kahan_add<A, T>(a[st], cz[st].x * w[st], cz[st].y * w[st]);
+            else acc_add<A, T>(a[st], cz[st].x * w[st], cz[st].y * w[st]);
+            acc[off[st]] = a[st];
+          }
+        }
+        meta_c = meta_n;
       }
     }
     __syncthreads();

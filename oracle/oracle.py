@@ -419,8 +419,13 @@ def ndft_adjoint(k, N, fhat, subset=None):
 
 
 def rel_l2(x, ref):
+    """||x - ref|| / ||ref|| in FP64: raw window sums reach 1e21 in 3-D (the
+    window is unnormalised), so FP32 squares would overflow."""
     x = np.asarray(x).ravel()
     ref = np.asarray(ref).ravel()
+    up = np.complex128 if (np.iscomplexobj(x) or np.iscomplexobj(ref)) else np.float64
+    x = x.astype(up)
+    ref = ref.astype(up)
     return float(np.linalg.norm(x - ref) / np.linalg.norm(ref))
 
 

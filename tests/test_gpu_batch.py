@@ -100,3 +100,45 @@ def test_batch_rejects_mismatched_and_stale():
         batch.forward(fs)
     with pytest.raises(nf.DimensionMismatch):
         nf.NFFTBatch([a]).forward(fs)
+
+
+def config4_plans(seed=4, nplans=64):
+    """64 2-D FP32 plans: N_i from {64, 96, 128, 192, 256, 384, 512} (grids of
+    2 N_i, radix-3 sizes included), M_i = floor(10^U(4, 6)), nodes U[-1/2, 1/2)^2,
+    Kaiser-Bessel m = 4, sigma = 2."""
+    rng = np.random.default_rng(seed)
+    sizes = [64, 96, 128, 192, 256, 384, 512]
+    out = []
+    for _ in range(nplans):
+        n = int(rng.choice(sizes))
+        M = int(10 ** rng.uniform(4, 6))
+        k = (rng.random((2, M)) - 0.5).astype(np.float32)
+        out.append((k, (n, n)))
+    return out
+
+
+def test_batch_config4_64_plans():
+    probs = config4_plans()
+    plans = [nf.plan_nfft(k, N, m=4, sigma=2.0) for k, N in probs]
+    batch = nf.NFFTBatch(plans)
+    rng = np.random.default_rng(9)
+    fs = [nf.as_colmajor((rng.standard_normal(N) + 1j * rng.standard_normal(N)).astype(np.complex64), N,
+                         torch.complex64) for _, N in probs]
+    vs = [torch.as_tensor((rng.standard_normal(k.shape[1]) + 1j * rng.standard_normal(k.shape[1]))
+                          .astype(np.complex64)).cuda() for k, _ in probs]
+    ys = batch.forward(fs)
+    xs = batch.adjoint(vs)
+    for i, (p, (k, N)) in enumerate(zip(plans, probs)):
+        assert oracle.rel_l2(ys[i].cpu().numpy(), (p * fs[i]).cpu().numpy()) <= 1e-6, i
+        assert oracle.rel_l2(xs[i].cpu().numpy(), (nf.adjoint(p) * vs[i]).cpu().numpy()) <= 1e-6, i
+    # accuracy against the FP64 NDFT on node / frequency subsets of a few plans
+    for i in (0, 17, 63):
+        k, N = probs[i]
+        k64 = k.astype(np.float64)
+        f = fs[i].cpu().numpy().astype(np.complex128)
+        sub = np.random.default_rng(i).choice(k.shape[1], 64, replace=False)
+        ref = oracle.ndft_forward(k64, f, subset=sub)
+        assert oracle.rel_l2(ys[i].cpu().numpy()[sub], ref) < 1e-5, i
+        lin = np.random.default_rng(i + 1).choice(N[0] * N[1], 32, replace=False)
+        refx = oracle.ndft_adjoint(k64, N, vs[i].cpu().numpy().astype(np.complex128), subset=lin)
+        assert oracle.rel_l2(xs[i].cpu().numpy().ravel(order="F")[lin], refx) < 1e-5, i
