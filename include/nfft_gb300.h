@@ -261,6 +261,24 @@ int nfft_batch_destroy(nfft_batch* batch);
 int nfft_batch_forward(nfft_batch* batch, const void* const* f, void* const* fhat);
 int nfft_batch_adjoint(nfft_batch* batch, const void* const* fhat, void* const* f);
 
+/* Directional plans: NFFTPlan(k, N; dims) (src/implementation.jl:73-104,
+ * src/directional.jl) -- the NFFT along the contiguous dimensions
+ * dim_lo..dim_hi (0-based, inclusive) of a D-dimensional array (D <= 3), every
+ * other index a batch column.  k is (dim_hi-dim_lo+1) x M; node values are
+ * arrays of size NOut = N with the dims range replaced by M (column-major).
+ * precompute is LINEAR and the loops unblocked, as in the reference; params
+ * supplies m, sigma and the window.  forward: f (N) -> fhat (NOut);
+ * adjoint: fhat (NOut) -> f (N).  nfft_dplan_set_nodes checks the nodes
+ * like checkNodes and synchronises the stream. */
+typedef struct nfft_dplan nfft_dplan;
+int nfft_dplan_create(nfft_dplan** plan, int precision, int D, const int64_t* N, int dim_lo, int dim_hi, int64_t M,
+                      const nfft_params* params, void* stream);
+int nfft_dplan_destroy(nfft_dplan* plan);
+int nfft_dplan_set_nodes(nfft_dplan* plan, const void* k, int k_on_device);
+int nfft_dplan_set_stream(nfft_dplan* plan, void* stream);
+int nfft_dplan_forward(nfft_dplan* plan, const void* f, void* fhat);
+int nfft_dplan_adjoint(nfft_dplan* plan, const void* fhat, void* f);
+
 /* Wait for the plan's stream. */
 int nfft_sync(nfft_plan* plan);
 

@@ -7,5 +7,6 @@ from .plan import (  # noqa: F401
     FULL, LINEAR, POLYNOMIAL, TENSOR, WINDOWS, AdjointPlan, ArgumentError, DimensionMismatch, GB300NFFTPlan,
     NFFTError, NFFTParams, PrecomputeFlags, TimingStats, accuracy_params, adjoint, as_colmajor, convolve_,
     convolve_transpose_, deconvolve_, deconvolve_transpose_, empty_image, kernel_launch_count, mul_, nfft,
-    nfft_adjoint, NFFTBatch, nodes_, params_to_reltol, plan_nfft, reltol_to_params, size_in, size_out)
+    nfft_adjoint, GB300DirectionalPlan, NFFTBatch, nodes_, params_to_reltol, plan_nfft, reltol_to_params, size_in,
+    size_out)
 from ._lib import LIB_PATH, exported_symbols, load  # noqa: F401

@@ -94,6 +94,12 @@ SIGNATURES = {
     "nfft_batch_destroy": (_I, [_P]),
     "nfft_batch_forward": (_I, [_P, _P, _P]),
     "nfft_batch_adjoint": (_I, [_P, _P, _P]),
+    "nfft_dplan_create": (_I, [_P, _I, _I, _I64P, _I, _I, _I64, _P, _P]),
+    "nfft_dplan_destroy": (_I, [_P]),
+    "nfft_dplan_set_nodes": (_I, [_P, _P, _I]),
+    "nfft_dplan_set_stream": (_I, [_P, _P]),
+    "nfft_dplan_forward": (_I, [_P, _P, _P]),
+    "nfft_dplan_adjoint": (_I, [_P, _P, _P]),
     "nfft_kernel_launch_count": (_I64, []),
     "nfft_status_string": (ctypes.c_char_p, [_I]),
     "nfft_last_error": (ctypes.c_char_p, []),

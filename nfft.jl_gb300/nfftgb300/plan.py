@@ -526,7 +526,10 @@ class AdjointPlan:
             fHat = torch.as_tensor(np.asarray(fHat))
         if tuple(fHat.shape) != p.NOut:
             raise DimensionMismatch("Data is not consistent with NFFTPlan")
-        fHat = fHat.to(device=p.device, dtype=p.cdtype).contiguous()
+        if len(p.NOut) > 1:  # directional plans: column-major node-value arrays
+            fHat = as_colmajor(fHat, p.NOut, p.cdtype, p.device)
+        else:
+            fHat = fHat.to(device=p.device, dtype=p.cdtype).contiguous()
         f = empty_image(p.N, p.cdtype, p.device)
         return p.adjoint_(f, fHat)
 
@@ -559,6 +562,11 @@ def plan_nfft(*args, **kwargs):
     timing = kwargs.get("timing")
     if isinstance(N, int):
         N = (N,)
+    dims = kwargs.pop("dims", None)
+    if dims is not None:
+        r = _dims_range(dims, len(N))
+        if r != (1, len(N)):
+            return GB300DirectionalPlan(k, N, dims=r, **kwargs)
     p = GB300NFFTPlan(k, N, **kwargs)
     if timing is not None:
         timing.pre = p._timing.pre if p._timing is not None else 0.0
@@ -699,3 +707,160 @@ class NFFTBatch:
         outs = [empty_image(p.N, p.cdtype, p.device) for p in self.plans]
         return self.adjoint_(outs, [v.to(device=p.device, dtype=p.cdtype).contiguous()
                                     for p, v in zip(self.plans, fHats)])
+
+
+def _dims_range(dims, D):
+    """dims as an Integer or a UnitRange (1-based, inclusive) -> (lo, hi)."""
+    if isinstance(dims, (int, np.integer)):
+        lo = hi = int(dims)
+    elif isinstance(dims, range):
+        if dims.step != 1 or len(dims) == 0:
+            raise ArgumentError("dims must be a contiguous range")
+        lo, hi = dims.start, dims.stop - 1
+    else:
+        d = [int(x) for x in np.atleast_1d(dims)]
+        if d != list(range(d[0], d[0] + len(d))):
+            raise ArgumentError("dims must be a contiguous range")
+        lo, hi = d[0], d[-1]
+    if lo < 1 or hi > D:
+        raise ArgumentError(f"dims {lo}:{hi} do not fit a {D}-dimensional array")
+    return lo, hi
+
+
+class GB300DirectionalPlan:
+    """NFFTPlan with ``dims`` (src/directional.jl, src/implementation.jl:73-104):
+    the NFFT along the contiguous dimensions ``dims`` of an array of size N,
+    every other index a batch column.  ``k`` is len(dims) x J; NOut is N with
+    the dims range replaced by J.  precompute is LINEAR, as in the reference.
+    Node-value arrays (fHat) are column-major of shape NOut."""
+
+    def __init__(self, k, N, *, dims, m=None, sigma=None, reltol=None, window="kaiser_bessel",
+                 precompute=None, blocking=None, sortNodes=False, storeDeconvolutionIdx=False, blockSize=None,
+                 compensated=False, timing=None, fftflags=None, device="cuda"):
+        kk = GB300NFFTPlan._nodes_array(k)
+        N = tuple(int(n) for n in N)
+        lo, hi = dims
+        R = hi - lo + 1
+        if kk.shape[0] != R:
+            raise ArgumentError(f"Nodes x have dimension {kk.shape[0]} != {R}")
+        if len(N) > 3:
+            raise NotImplementedError("directional plans support arrays of up to 3 dimensions")
+        if window not in WINDOWS:
+            raise NotImplementedError(f"Window {window} not yet implemented!")
+        m_, s_, r_ = accuracy_params(m, sigma, reltol)
+        dt = kk.dtype if isinstance(kk, np.ndarray) else {torch.float32: np.float32,
+                                                          torch.float64: np.float64}[kk.dtype]
+        self.precision = 32 if dt == np.float32 else 64
+        self.dtype = torch.float32 if self.precision == 32 else torch.float64
+        self.cdtype = torch.complex64 if self.precision == 32 else torch.complex128
+        dev = torch.device(device)
+        if dev.type == "cuda" and dev.index is None:
+            dev = torch.device("cuda", torch.cuda.current_device())
+        self.device = dev
+        self.N = N
+        self.dims = tuple(range(lo, hi + 1))
+        self.J = int(kk.shape[1])
+        self.NOut = N[:lo - 1] + (self.J,) + N[hi:]
+        self.params = NFFTParams(m=m_, sigma=s_, reltol=r_, window=window, precompute=PrecomputeFlags.LINEAR,
+                                 sortNodes=bool(sortNodes), storeDeconvolutionIdx=bool(storeDeconvolutionIdx),
+                                 blocking=False, blockSize=tuple(blockSize or ()), compensated=False)
+        lib = L.load()
+        prm = L.nfft_params()
+        lib.nfft_params_default(ctypes.byref(prm))
+        prm.m = m_
+        prm.sigma = s_
+        prm.window = WINDOWS[window]
+        prm.precompute = int(PrecomputeFlags.LINEAR)
+        prm.blocking = 0
+        Narr = (ctypes.c_int64 * 3)(*(list(N) + [1] * (3 - len(N))))
+        h = ctypes.c_void_p()
+        with torch.cuda.device(dev):
+            stream = torch.cuda.current_stream(dev)
+            _check(lib.nfft_dplan_create(ctypes.byref(h), self.precision, len(N), Narr, lo - 1, hi - 1, self.J,
+                                         ctypes.byref(prm), ctypes.c_void_p(stream.cuda_stream)))
+        self._handle = h
+        self._stream = stream.cuda_stream
+        sig = 2.0 * ((int(np.ceil(s_ * N[lo - 1])) // 2)) / N[lo - 1]
+        self.params.sigma = sig
+        self.Ñ = tuple(2 * (int(np.ceil(s_ * n)) // 2) if lo - 1 <= d <= hi - 1 else n for d, n in enumerate(N))
+        self.Ntilde = self.Ñ
+        self.nodes_(kk)
+
+    def __del__(self):
+        h = getattr(self, "_handle", None)
+        if h is not None and h.value:
+            try:
+                L.load().nfft_dplan_destroy(h)
+            except Exception:
+                pass
+            self._handle = None
+
+    def _sync_stream(self):
+        s = torch.cuda.current_stream(self.device).cuda_stream
+        if s != self._stream:
+            _check(L.load().nfft_dplan_set_stream(self._handle, ctypes.c_void_p(s)))
+            self._stream = s
+
+    def nodes_(self, k):
+        kk = GB300NFFTPlan._nodes_array(k)
+        if kk.shape[0] != len(self.dims):
+            raise ArgumentError(f"Nodes x have dimension {kk.shape[0]} != {len(self.dims)}")
+        if kk.shape[1] != self.J:
+            raise DimensionMismatch("nodes! on a directional plan keeps the node count")
+        self._sync_stream()
+        lib = L.load()
+        if isinstance(kk, torch.Tensor):
+            kt = kk.to(device=self.device, dtype=self.dtype).t().contiguous()
+            rc = lib.nfft_dplan_set_nodes(self._handle, _ptr(kt), 1)
+        else:
+            kc = np.ascontiguousarray(kk.T.astype(np.float32 if self.precision == 32 else np.float64))
+            rc = lib.nfft_dplan_set_nodes(self._handle, ctypes.c_void_p(kc.ctypes.data), 0)
+        _check(rc)
+        self.k = kk
+        return self
+
+    def size_in(self):
+        return self.N
+
+    def size_out(self):
+        return self.NOut
+
+    def _arr(self, x, shape):
+        if not isinstance(x, torch.Tensor) or tuple(x.shape) != shape:
+            raise DimensionMismatch("Data is not consistent with NFFTPlan")
+        if x.dtype != self.cdtype or x.device != self.device or not _is_colmajor(x):
+            raise ArgumentError(f"arrays must be column-major {self.cdtype} tensors on {self.device}")
+        return x
+
+    def forward_(self, fHat, f):
+        f = self._arr(f, self.N)
+        fHat = self._arr(fHat, self.NOut)
+        self._sync_stream()
+        _check(L.load().nfft_dplan_forward(self._handle, _ptr(f), _ptr(fHat)))
+        return fHat
+
+    def adjoint_(self, f, fHat):
+        f = self._arr(f, self.N)
+        fHat = self._arr(fHat, self.NOut)
+        self._sync_stream()
+        _check(L.load().nfft_dplan_adjoint(self._handle, _ptr(fHat), _ptr(f)))
+        return f
+
+    def __mul__(self, f):
+        f = as_colmajor(f, self.N, self.cdtype, self.device)
+        return self.forward_(empty_image(self.NOut, self.cdtype, self.device), f)
+
+    def adjoint(self):
+        return AdjointPlan(self)
+
+    @property
+    def H(self):
+        return AdjointPlan(self)
+
+    def copy(self):
+        return GB300DirectionalPlan(self.k, self.N, dims=(self.dims[0], self.dims[-1]), m=self.params.m,
+                                    sigma=self.params.sigma, window=self.params.window, device=self.device)
+
+    def __repr__(self):
+        return (f"GB300DirectionalPlan with {self.J} sampling points for an input array of size{self.N} and an "
+                f"output array of size{self.NOut} with dims {self.dims}")
