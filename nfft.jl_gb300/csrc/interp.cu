@@ -2,8 +2,10 @@
 // of prod_d phi_d * g[tap], src/convolution.jl:229-344 (blocked) and :56-99.
 //
 // Warp per node (D >= 2) or 32/G nodes per warp (D = 1), nodes visited in
-// bin-sorted order so that neighbouring warps read overlapping grid
-// neighbourhoods through L1/L2.  Window values come from the stored window
+// bin-sorted order; for D >= 2 each CTA takes a contiguous chunk of the
+// sorted nodes, so the nodes an SM visits close in time read overlapping grid
+// neighbourhoods through L1, and a warp issues all of a node's grid loads
+// before its sums (memory-level parallelism).  Window values come from the stored window
 // tensor (TENSOR / FULL / LINEAR) or from the fitted polynomial evaluated with
 // its coefficients held in registers (POLYNOMIAL).  Grid offsets within a
 // plane are 32-bit; the plane offset is 64-bit.
@@ -13,6 +15,16 @@ namespace nfft {
 namespace {
 
 constexpr int kInterpThreads = 256;
+
+// 8- or 16-byte asynchronous global -> shared copy (cp.async, sm_80+).
+template <typename C> __device__ __forceinline__ void cp_async_elem(C* smem, const C* gmem) {
+  const unsigned s = static_cast<unsigned>(__cvta_generic_to_shared(smem));
+  if constexpr (sizeof(C) == 8)
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(s), "l"(gmem) : "memory");
+  else
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
 
 template <int D, int L, typename T, bool TABLE>
 __global__ void __launch_bounds__(kInterpThreads) interp_kernel(Geom<T> G, Nodes<T> Nd,
@@ -70,7 +82,13 @@ __global__ void __launch_bounds__(kInterpThreads) interp_kernel(Geom<T> G, Nodes
   } else {
     PolyRegs<D, L, T> P;
     if constexpr (!TABLE) P.load(G.coeffs, lane);
-    for (int64_t i = warp_global; i < Nd.M; i += warps_total) interp_node<D, L, T, TABLE>(G, Nd, P, i, lane, g, fhat);
+    // each CTA takes a contiguous chunk of the bin-sorted nodes: nodes a CTA
+    // visits close in time share their grid neighbourhood in L1
+    const int64_t chunk = (Nd.M + gridDim.x - 1) / gridDim.x;
+    const int64_t lo = int64_t(blockIdx.x) * chunk;
+    const int64_t hi = lo + chunk < Nd.M ? lo + chunk : Nd.M;
+    for (int64_t i = lo + (threadIdx.x >> 5); i < hi; i += blockDim.x >> 5)
+      interp_node<D, L, T, TABLE>(G, Nd, P, i, lane, g, fhat);
   }
 }
 
@@ -102,17 +120,28 @@ __global__ void __launch_bounds__(kInterpThreads) interp_tile_kernel(Geom<T> G, 
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
   const int m1 = G.m - 1;
   const bool small = G.small_grid;
-  // stage the padded tile
-  for (int r = warp; r < P1 * P2; r += nwarps) {
-    const int y = r % P1, z = r / P1;
-    const int gy = D >= 2 ? (small ? wrap_any(o1 - m1 + y, G.Nt[1]) : wrap_once(o1 - m1 + y, G.Nt[1])) : 0;
-    const int gz = D == 3 ? (small ? wrap_any(o2 - m1 + z, G.Nt[2]) : wrap_once(o2 - m1 + z, G.Nt[2])) : 0;
-    const C* grow = g + int64_t(gz) * G.plane + int64_t(gy) * G.Nt[0];
-    C* srow = tile + z * plane + y * pitch;
-    for (int x = lane; x < P0; x += 32) {
-      const int gx = small ? wrap_any(o0 - m1 + x, G.Nt[0]) : wrap_once(o0 - m1 + x, G.Nt[0]);
-      srow[x] = __ldg(grow + gx);
+  // stage the padded tile with asynchronous copies (cp.async): every row
+  // copy is issued before the single wait, so a warp keeps all of its rows'
+  // loads in flight instead of one load-store round trip per row
+  {
+    const int rows = P1 * P2;
+    int r = warp, y = r % P1, z = r / P1;
+    for (; r < rows; r += nwarps) {
+      const int gy = D >= 2 ? (small ? wrap_any(o1 - m1 + y, G.Nt[1]) : wrap_once(o1 - m1 + y, G.Nt[1])) : 0;
+      const int gz = D == 3 ? (small ? wrap_any(o2 - m1 + z, G.Nt[2]) : wrap_once(o2 - m1 + z, G.Nt[2])) : 0;
+      const C* grow = g + int64_t(gz) * G.plane + int64_t(gy) * G.Nt[0];
+      C* srow = tile + z * plane + y * pitch;
+      for (int x = lane; x < P0; x += 32) {
+        const int gx = small ? wrap_any(o0 - m1 + x, G.Nt[0]) : wrap_once(o0 - m1 + x, G.Nt[0]);
+        cp_async_elem(srow + x, grow + gx);
+      }
+      y += nwarps;
+      while (y >= P1) {
+        y -= P1;
+        ++z;
+      }
     }
+    cp_async_wait_all();
   }
   __syncthreads();
   if constexpr (D == 1) {

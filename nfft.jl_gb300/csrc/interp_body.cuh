@@ -44,17 +44,23 @@ __device__ __forceinline__ void interp_node(const Geom<T>& G, const Nodes<T>& Nd
       ai = fma(wxy[s], v.y, ai);
     }
   } else {
+    // all of the node's grid loads first (memory-level parallelism), then the sums
+    C v[L][LN::NSTEP];
 #pragma unroll
     for (int iz = 0; iz < L; ++iz) {
-      const T wz = wsel<D, L>(W, 2 * L + iz);
       const int gz = small ? wrap_any(nd.z - m + 1 + iz, G.Nt[2]) : wrap_once(nd.z - m + 1 + iz, G.Nt[2]);
       const C* gp = g + int64_t(gz) * G.plane;
 #pragma unroll
+      for (int s = 0; s < LN::NSTEP; ++s) v[iz][s] = __ldg(gp + row[s]);
+    }
+#pragma unroll
+    for (int iz = 0; iz < L; ++iz) {
+      const T wz = wsel<D, L>(W, 2 * L + iz);
+#pragma unroll
       for (int s = 0; s < LN::NSTEP; ++s) {
-        const C v = __ldg(gp + row[s]);
         const T w = wxy[s] * wz;
-        ar = fma(w, v.x, ar);
-        ai = fma(w, v.y, ai);
+        ar = fma(w, v[iz][s].x, ar);
+        ai = fma(w, v[iz][s].y, ai);
       }
     }
   }
