@@ -1,0 +1,536 @@
+// Pruned grid FFT fused with the deconvolution (D = 2, 3; every Ntilde_d a
+// power of two in [64, 1024]).  Replaces, on the transform path,
+//   forward:  fill!(tmpVec, 0); deconvolve!; fft!      (src/implementation.jl:159-161)
+//   adjoint:  bfft!; deconvolve_transpose!             (:182-183)
+// by line FFTs that touch only what the zero padding leaves nonzero:
+//   forward  X: one kernel reads the image rows, applies the separable
+//               deconvolution factors, places each row into its zero-padded
+//               length-Ntilde_0 line and transforms it (only image rows, y and
+//               z inside the image);
+//            Y: lines along y of the image z-slices, input read only at the
+//               image rows (the others are zero), all outputs written;
+//            Z: lines along z of every (x, y), input read only at the image
+//               slices, all outputs written.
+//   adjoint  Z', Y': the same lines backwards, writing only the outputs the
+//               next step reads; X': transforms the image rows and writes the
+//               cropped, deconvolved image.
+// The grid ends up (forward) or is read (adjoint) exactly as the unpruned
+// transform of the zero-padded grid.  Each CTA transforms W lines held in a
+// shared-memory tile [position][line] (row pitch W+1: transfers along a line
+// and butterflies across lines are both free of bank conflicts) with
+// radix-8 Stockham passes (a final radix-2 or radix-4 pass for 128, 256,
+// 1024) computed in registers; twiddles come from a per-length table
+// exp(-2 pi i q / n) built on the host in FP64.  Unnormalised, forward sign
+// -1 / backward +1, like FFTW's fft!/bfft!.
+#include "nfft_internal.cuh"
+
+#include <cmath>
+#include <cstdlib>
+#include <cstring>
+#include <vector>
+
+namespace nfft {
+namespace {
+
+constexpr int kFftThreads = 256;
+
+template <typename T> using Cx = typename Cplx<T>::type;
+
+template <typename C> __device__ __forceinline__ C c_add(C a, C b) {
+  a.x += b.x;
+  a.y += b.y;
+  return a;
+}
+template <typename C> __device__ __forceinline__ C c_sub(C a, C b) {
+  a.x -= b.x;
+  a.y -= b.y;
+  return a;
+}
+template <typename C> __device__ __forceinline__ C c_mul(C a, C b) {
+  C r;
+  r.x = a.x * b.x - a.y * b.y;
+  r.y = a.x * b.y + a.y * b.x;
+  return r;
+}
+// a * (S i), S = -1 (forward) or +1 (backward)
+template <int S, typename C> __device__ __forceinline__ C c_mul_si(C a) {
+  C r;
+  r.x = S > 0 ? -a.y : a.y;
+  r.y = S > 0 ? a.x : -a.x;
+  return r;
+}
+
+// In-register DFTs of length 2, 4, 8 with kernel exp(S 2 pi i t q / R),
+// outputs in natural order.
+template <int S, typename C> __device__ __forceinline__ void dft2(C (&v)[2]) {
+  const C a = v[0];
+  v[0] = c_add(a, v[1]);
+  v[1] = c_sub(a, v[1]);
+}
+template <int S, typename C> __device__ __forceinline__ void dft4(C (&u)[4]) {
+  const C c0 = c_add(u[0], u[2]), c1 = c_sub(u[0], u[2]);
+  const C d0 = c_add(u[1], u[3]), d1 = c_mul_si<S>(c_sub(u[1], u[3]));
+  u[0] = c_add(c0, d0);
+  u[2] = c_sub(c0, d0);
+  u[1] = c_add(c1, d1);
+  u[3] = c_sub(c1, d1);
+}
+template <int S, typename C> __device__ __forceinline__ void dft8(C (&v)[8]) {
+  using T = decltype(v[0].x);
+  const T h = T(0.70710678118654752440084436210485);  // 1/sqrt(2)
+  C a[4], b[4];
+#pragma unroll
+  for (int t = 0; t < 4; ++t) {
+    a[t] = c_add(v[t], v[t + 4]);
+    b[t] = c_sub(v[t], v[t + 4]);
+  }
+  // b[t] *= w^t, w = exp(S i pi / 4) = h (1 + S i)
+  {
+    const C s1 = c_mul_si<S>(b[1]);
+    b[1].x = h * (b[1].x + s1.x);
+    b[1].y = h * (b[1].y + s1.y);
+    b[2] = c_mul_si<S>(b[2]);
+    const C s3 = c_mul_si<S>(b[3]);
+    b[3].x = h * (s3.x - b[3].x);
+    b[3].y = h * (s3.y - b[3].y);
+  }
+  dft4<S>(a);
+  dft4<S>(b);
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    v[2 * q] = a[q];
+    v[2 * q + 1] = b[q];
+  }
+}
+template <int S, int R, typename C> __device__ __forceinline__ void dft(C (&v)[R]) {
+  if constexpr (R == 8) dft8<S>(v);
+  else if constexpr (R == 4) dft4<S>(v);
+  else dft2<S>(v);
+}
+
+// One Stockham pass over the W lines of length N in buf[pos * (W + 1) + w]:
+// butterfly j of line w loads positions j + r N/R, twiddles by
+// (j mod NS) r / (NS R) turns, transforms, and stores at
+// (j div NS) NS R + (j mod NS) + r NS.
+template <typename T, int S, int N, int W, int R, int NS>
+__device__ __forceinline__ void fft_pass(Cx<T>* buf, const Cx<T>* __restrict__ tw) {
+  using C = Cx<T>;
+  constexpr int NB = N / R;
+  constexpr int TOT = NB * W;
+  constexpr int BPT = (TOT + kFftThreads - 1) / kFftThreads;
+  constexpr int P = W + 1;
+  C v[BPT][R];
+#pragma unroll
+  for (int b = 0; b < BPT; ++b) {
+    const int t = threadIdx.x + b * kFftThreads;
+    if (TOT % kFftThreads == 0 || t < TOT) {
+      const int w = t % W, j = t / W;
+#pragma unroll
+      for (int r = 0; r < R; ++r) v[b][r] = buf[(j + r * NB) * P + w];
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int b = 0; b < BPT; ++b) {
+    const int t = threadIdx.x + b * kFftThreads;
+    if (TOT % kFftThreads == 0 || t < TOT) {
+      const int w = t % W, j = t / W;
+      const int k = j & (NS - 1);
+      if constexpr (NS > 1) {
+        constexpr int STEP = N / (NS * R);
+#pragma unroll
+        for (int r = 1; r < R; ++r) {
+          C tt = __ldg(tw + ((k * r * STEP) & (N - 1)));
+          if constexpr (S > 0) tt.y = -tt.y;
+          v[b][r] = c_mul(v[b][r], tt);
+        }
+      }
+      dft<S, R>(v[b]);
+      const int base = (j - k) * R + k;
+#pragma unroll
+      for (int r = 0; r < R; ++r) buf[(base + r * NS) * P + w] = v[b][r];
+    }
+  }
+  __syncthreads();
+}
+
+template <typename T, int S, int N, int W, int NS = 1>
+__device__ __forceinline__ void fft_lines(Cx<T>* buf, const Cx<T>* __restrict__ tw) {
+  if constexpr (NS < N) {
+    constexpr int REM = N / NS;
+    constexpr int R = REM % 8 == 0 ? 8 : REM;
+    fft_pass<T, S, N, W, R, NS>(buf, tw);
+    fft_lines<T, S, N, W, NS * R>(buf, tw);
+  }
+}
+
+// Move the W x n tile elements q = threadIdx.x + i * kFftThreads through
+// registers in batches of up to 16: every load of a batch is issued before
+// its stores, so a thread keeps a batch of global (or shared) loads in flight
+// instead of one load-store round trip per element.
+template <typename C, int ITEMS, typename Load, typename Store>
+__device__ __forceinline__ void staged_copy(Load ld, Store st) {
+  constexpr int CH = ITEMS < 16 ? ITEMS : 16;
+  static_assert(ITEMS % CH == 0, "tile items per thread");
+#pragma unroll 1
+  for (int c0 = 0; c0 < ITEMS; c0 += CH) {
+    C v[CH];
+#pragma unroll
+    for (int i = 0; i < CH; ++i) v[i] = ld(int(threadIdx.x) + (c0 + i) * kFftThreads);
+#pragma unroll
+    for (int i = 0; i < CH; ++i) st(int(threadIdx.x) + (c0 + i) * kFftThreads, v[i]);
+  }
+}
+
+// Two CTAs per SM (registers capped at 128) where the tile's registers fit
+// without spilling; one for the largest lines.
+template <typename T, int N> constexpr int fft_min_blocks() { return (sizeof(T) == 4 ? N <= 512 : N <= 256) ? 2 : 1; }
+
+struct FftGeom {
+  int N[3], Nt[3];
+  int64_t plane;  // Nt0 * Nt1
+};
+
+template <typename T> struct Inv3 {
+  const T* d[3];
+};
+
+// forward X: image rows -> deconvolved, zero-padded, transformed grid rows
+template <typename T, int NX, int W>
+__global__ void __launch_bounds__(kFftThreads, fft_min_blocks<T, NX>()) fft_x_pad_kernel(FftGeom G, Inv3<T> inv, const Cx<T>* __restrict__ f,
+                                                                Cx<T>* __restrict__ g, const Cx<T>* __restrict__ tw) {
+  using C = Cx<T>;
+  extern __shared__ __align__(16) unsigned char fft_smem[];
+  C* buf = reinterpret_cast<C*>(fft_smem);
+  constexpr int P = W + 1;
+  const int64_t rows = int64_t(G.N[1]) * G.N[2];
+  const int64_t r0 = int64_t(blockIdx.x) * W;
+  const int N0 = G.N[0], h0 = G.N[0] / 2;
+  constexpr int ITEMS = NX * W / kFftThreads;
+  // per row: the y / z deconvolution factor and the grid row offset
+  __shared__ T s_row[W];
+  __shared__ int64_t s_goff[W];
+  if (threadIdx.x < W) {
+    const int64_t r = r0 + threadIdx.x;
+    T s = T(0);
+    int64_t go = 0;
+    if (r < rows) {
+      const int y = int(r % G.N[1]), z = int(r / G.N[1]);
+      s = __ldg(inv.d[1] + y) * __ldg(inv.d[2] + z);
+      go = int64_t(NX) * (wrap_once(y - G.N[1] / 2, G.Nt[1]) +
+                          int64_t(G.Nt[1]) * wrap_once(z - G.N[2] / 2, G.Nt[2]));
+    }
+    s_row[threadIdx.x] = s;
+    s_goff[threadIdx.x] = go;
+  }
+  __syncthreads();
+  staged_copy<C, ITEMS>(
+      [&](int q) {
+        const int pos = q % NX, w = q / NX;
+        const int nx = wrap_once(pos + h0, NX);
+        C v;
+        v.x = T(0);
+        v.y = T(0);
+        if (r0 + w < rows && nx < N0) v = f[nx + int64_t(N0) * (r0 + w)];
+        return v;
+      },
+      [&](int q, C v) {
+        const int pos = q % NX, w = q / NX;
+        const int nx = wrap_once(pos + h0, NX);
+        const T s = nx < N0 ? __ldg(inv.d[0] + nx) * s_row[w] : T(0);
+        v.x *= s;
+        v.y *= s;
+        buf[pos * P + w] = v;
+      });
+  __syncthreads();
+  fft_lines<T, -1, NX, W>(buf, tw);
+  staged_copy<C, ITEMS>([&](int q) { return buf[(q % NX) * P + q / NX]; },
+                        [&](int q, C v) {
+                          if (r0 + q / NX < rows) g[s_goff[q / NX] + q % NX] = v;
+                        });
+}
+
+// adjoint X': grid rows of the image -> transformed, cropped, deconvolved image rows
+template <typename T, int NX, int W>
+__global__ void __launch_bounds__(kFftThreads, fft_min_blocks<T, NX>()) fft_x_crop_kernel(FftGeom G, Inv3<T> inv, const Cx<T>* __restrict__ g,
+                                                                 Cx<T>* __restrict__ f, const Cx<T>* __restrict__ tw) {
+  using C = Cx<T>;
+  extern __shared__ __align__(16) unsigned char fft_smem[];
+  C* buf = reinterpret_cast<C*>(fft_smem);
+  constexpr int P = W + 1;
+  const int64_t rows = int64_t(G.N[1]) * G.N[2];
+  const int64_t r0 = int64_t(blockIdx.x) * W;
+  const int N0 = G.N[0], h0 = G.N[0] / 2;
+  constexpr int ITEMS = NX * W / kFftThreads;
+  __shared__ T s_row[W];
+  __shared__ int64_t s_goff[W];
+  if (threadIdx.x < W) {
+    const int64_t r = r0 + threadIdx.x;
+    T s = T(0);
+    int64_t go = 0;
+    if (r < rows) {
+      const int y = int(r % G.N[1]), z = int(r / G.N[1]);
+      s = __ldg(inv.d[1] + y) * __ldg(inv.d[2] + z);
+      go = int64_t(NX) * (wrap_once(y - G.N[1] / 2, G.Nt[1]) +
+                          int64_t(G.Nt[1]) * wrap_once(z - G.N[2] / 2, G.Nt[2]));
+    }
+    s_row[threadIdx.x] = s;
+    s_goff[threadIdx.x] = go;
+  }
+  __syncthreads();
+  staged_copy<C, ITEMS>(
+      [&](int q) {
+        C v;
+        v.x = T(0);
+        v.y = T(0);
+        if (r0 + q / NX < rows) v = g[s_goff[q / NX] + q % NX];
+        return v;
+      },
+      [&](int q, C v) { buf[(q % NX) * P + q / NX] = v; });
+  __syncthreads();
+  fft_lines<T, 1, NX, W>(buf, tw);
+  staged_copy<C, ITEMS>([&](int q) { return buf[(q % NX) * P + q / NX]; },
+                        [&](int q, C v) {
+                          const int pos = q % NX, w = q / NX;
+                          const int nx = wrap_once(pos + h0, NX);
+                          if (r0 + w < rows && nx < N0) {
+                            const T s = __ldg(inv.d[0] + nx) * s_row[w];
+                            v.x *= s;
+                            v.y *= s;
+                            f[nx + int64_t(N0) * (r0 + w)] = v;
+                          }
+                        });
+}
+
+// Lines of length NL along an axis with element stride `stride`; a CTA takes
+// W consecutive x of one outer index.  The outer index o runs over the image
+// positions of a pruned outer dimension (outer_N > 0: grid index
+// (o - outer_N/2) mod outer_Nt) or over all grid positions (outer_N = 0).
+// FWD: input read only at the line's image positions (the rest is zero), all
+// outputs written.  Otherwise: all inputs read, only image positions written.
+struct LineGeom {
+  int64_t stride;       // elements between consecutive line positions
+  int64_t outer_stride; // elements between consecutive outer grid indices
+  int tiles_x;          // Nt0 / W
+  int n_img;            // image length along the line
+  int outer_N, outer_Nt;
+};
+
+template <typename T, int NL, int W, bool FWD>
+__global__ void __launch_bounds__(kFftThreads, fft_min_blocks<T, NL>()) fft_lines_kernel(LineGeom L, Cx<T>* __restrict__ g,
+                                                                const Cx<T>* __restrict__ tw) {
+  using C = Cx<T>;
+  extern __shared__ __align__(16) unsigned char fft_smem[];
+  C* buf = reinterpret_cast<C*>(fft_smem);
+  constexpr int P = W + 1;
+  const int tile = blockIdx.x % L.tiles_x;
+  const int o = blockIdx.x / L.tiles_x;
+  const int go = L.outer_N > 0 ? wrap_once(o - L.outer_N / 2, L.outer_Nt) : o;
+  C* base = g + int64_t(go) * L.outer_stride + int64_t(tile) * W;
+  const int head = L.n_img - L.n_img / 2;   // image positions [0, head) and [NL - n_img/2, NL)
+  const int tail0 = NL - L.n_img / 2;
+  constexpr int ITEMS = NL * W / kFftThreads;
+  staged_copy<C, ITEMS>(
+      [&](int q) {
+        const int w = q % W, pos = q / W;
+        C v;
+        v.x = T(0);
+        v.y = T(0);
+        if (!FWD || pos < head || pos >= tail0) v = base[int64_t(pos) * L.stride + w];
+        return v;
+      },
+      [&](int q, C v) { buf[(q / W) * P + q % W] = v; });
+  __syncthreads();
+  fft_lines<T, FWD ? -1 : 1, NL, W>(buf, tw);
+  staged_copy<C, ITEMS>([&](int q) { return buf[(q / W) * P + q % W]; },
+                        [&](int q, C v) {
+                          const int pos = q / W;
+                          if (FWD || pos < head || pos >= tail0) base[int64_t(pos) * L.stride + q % W] = v;
+                        });
+}
+
+template <typename T> constexpr int lines_per_cta() { return sizeof(T) == 4 ? 16 : 8; }
+
+template <int NL, typename T> size_t fft_smem_bytes() {
+  return size_t(NL) * (lines_per_cta<T>() + 1) * sizeof(Cx<T>);
+}
+
+FftGeom make_fft_geom(const nfft_plan* p) {
+  FftGeom G{};
+  for (int d = 0; d < 3; ++d) {
+    G.N[d] = int(p->N[d]);
+    G.Nt[d] = int(p->Nt[d]);
+  }
+  G.plane = p->Nt[0] * p->Nt[1];
+  return G;
+}
+
+template <typename T> Inv3<T> make_inv3(const nfft_plan* p) {
+  const T* inv = static_cast<const T*>(p->inv);
+  const T* one = inv + (p->N[0] + (p->D > 1 ? p->N[1] : 0) + (p->D > 2 ? p->N[2] : 0));
+  Inv3<T> I;
+  I.d[0] = inv;
+  I.d[1] = p->D > 1 ? inv + p->N[0] : one;
+  I.d[2] = p->D > 2 ? inv + p->N[0] + p->N[1] : one;
+  return I;
+}
+
+template <typename K> int set_smem(K kern, size_t bytes) {
+  NFFT_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(bytes)));
+  return NFFT_OK;
+}
+
+template <typename T, int NX> int x_pass_t(nfft_plan* p, const void* src, void* dst, bool fwd) {
+  using C = Cx<T>;
+  constexpr int W = lines_per_cta<T>();
+  const size_t smem = fft_smem_bytes<NX, T>();
+  const int64_t rows = p->N[1] * p->N[2];
+  const unsigned blocks = unsigned((rows + W - 1) / W);
+  const C* tw = static_cast<const C*>(p->fft_tw[0]);
+  if (fwd) {
+    auto kern = fft_x_pad_kernel<T, NX, W>;
+    if (int rc = set_smem(kern, smem)) return rc;
+    kern<<<blocks, kFftThreads, smem, p->stream>>>(make_fft_geom(p), make_inv3<T>(p), static_cast<const C*>(src),
+                                                   static_cast<C*>(dst), tw);
+  } else {
+    auto kern = fft_x_crop_kernel<T, NX, W>;
+    if (int rc = set_smem(kern, smem)) return rc;
+    kern<<<blocks, kFftThreads, smem, p->stream>>>(make_fft_geom(p), make_inv3<T>(p), static_cast<const C*>(src),
+                                                   static_cast<C*>(dst), tw);
+  }
+  NFFT_LAUNCH_CHECK();
+  return NFFT_OK;
+}
+
+template <typename T, int NL> int line_pass_t(nfft_plan* p, int axis, bool fwd) {
+  using C = Cx<T>;
+  constexpr int W = lines_per_cta<T>();
+  const size_t smem = fft_smem_bytes<NL, T>();
+  LineGeom L{};
+  L.tiles_x = int(p->Nt[0] / W);
+  L.n_img = int(p->N[axis]);
+  int64_t outer_count;
+  if (axis == 1) {  // y lines of the image z-slices (D = 3) or of the single plane (D = 2)
+    L.stride = p->Nt[0];
+    L.outer_stride = p->Nt[0] * p->Nt[1];
+    L.outer_N = p->D == 3 ? int(p->N[2]) : 0;
+    L.outer_Nt = int(p->Nt[2]);
+    outer_count = p->D == 3 ? p->N[2] : 1;
+  } else {          // z lines of every (x, y)
+    L.stride = p->Nt[0] * p->Nt[1];
+    L.outer_stride = p->Nt[0];
+    L.outer_N = 0;
+    L.outer_Nt = int(p->Nt[1]);
+    outer_count = p->Nt[1];
+  }
+  const unsigned blocks = unsigned(outer_count * L.tiles_x);
+  const C* tw = static_cast<const C*>(p->fft_tw[axis]);
+  C* g = static_cast<C*>(p->grid);
+  if (fwd) {
+    auto kern = fft_lines_kernel<T, NL, W, true>;
+    if (int rc = set_smem(kern, smem)) return rc;
+    kern<<<blocks, kFftThreads, smem, p->stream>>>(L, g, tw);
+  } else {
+    auto kern = fft_lines_kernel<T, NL, W, false>;
+    if (int rc = set_smem(kern, smem)) return rc;
+    kern<<<blocks, kFftThreads, smem, p->stream>>>(L, g, tw);
+  }
+  NFFT_LAUNCH_CHECK();
+  return NFFT_OK;
+}
+
+template <typename T> int x_pass(nfft_plan* p, const void* src, void* dst, bool fwd) {
+  switch (p->Nt[0]) {
+    case 64: return x_pass_t<T, 64>(p, src, dst, fwd);
+    case 128: return x_pass_t<T, 128>(p, src, dst, fwd);
+    case 256: return x_pass_t<T, 256>(p, src, dst, fwd);
+    case 512: return x_pass_t<T, 512>(p, src, dst, fwd);
+    case 1024: return x_pass_t<T, 1024>(p, src, dst, fwd);
+  }
+  set_error("fused FFT: unsupported length %lld", (long long)p->Nt[0]);
+  return NFFT_ERR_UNSUPPORTED;
+}
+
+template <typename T> int line_pass(nfft_plan* p, int axis, bool fwd) {
+  switch (p->Nt[axis]) {
+    case 64: return line_pass_t<T, 64>(p, axis, fwd);
+    case 128: return line_pass_t<T, 128>(p, axis, fwd);
+    case 256: return line_pass_t<T, 256>(p, axis, fwd);
+    case 512: return line_pass_t<T, 512>(p, axis, fwd);
+    case 1024: return line_pass_t<T, 1024>(p, axis, fwd);
+  }
+  set_error("fused FFT: unsupported length %lld", (long long)p->Nt[axis]);
+  return NFFT_ERR_UNSUPPORTED;
+}
+
+bool pow2_in_range(int64_t n) { return n >= 64 && n <= 1024 && (n & (n - 1)) == 0; }
+
+}  // namespace
+
+// Whether the plan's transforms take the fused pruned path; builds the
+// twiddle tables.  NFFT_GB300_FFT=cufft keeps cuFFT (and the separate
+// pad / crop kernels) for every plan created afterwards.
+int fused_fft_init(nfft_plan* p) {
+  p->fused_fft = false;
+  if (const char* e = getenv("NFFT_GB300_FFT"))
+    if (strcmp(e, "cufft") == 0) return NFFT_OK;
+  if (p->D < 2) return NFFT_OK;
+  for (int d = 0; d < p->D; ++d)
+    if (!pow2_in_range(p->Nt[d])) return NFFT_OK;
+  const size_t rs = p->real_size;
+  for (int d = 0; d < p->D; ++d) {
+    const int64_t n = p->Nt[d];
+    std::vector<double> h(2 * n);
+    for (int64_t q = 0; q < n; ++q) {
+      const double a = -2.0 * 3.14159265358979323846 * double(q) / double(n);
+      h[2 * q] = std::cos(a);
+      h[2 * q + 1] = std::sin(a);
+    }
+    std::vector<unsigned char> buf(2 * rs * n);
+    for (int64_t q = 0; q < 2 * n; ++q) {
+      if (rs == 4) reinterpret_cast<float*>(buf.data())[q] = float(h[q]);
+      else reinterpret_cast<double*>(buf.data())[q] = h[q];
+    }
+    if (cudaMalloc(&p->fft_tw[d], buf.size()) != cudaSuccess) {
+      set_error("cudaMalloc of FFT twiddles failed");
+      return NFFT_ERR_ALLOC;
+    }
+    NFFT_CUDA_TRY(cudaMemcpy(p->fft_tw[d], buf.data(), buf.size(), cudaMemcpyHostToDevice));
+  }
+  p->fused_fft = true;
+  return NFFT_OK;
+}
+
+// forward: image f -> transformed grid (pad + deconvolve + FFT).  The X
+// kernel is stage 1, the Y / Z line passes stage 2 (for the timing ring).
+int fused_forward_x(nfft_plan* p, const void* f) {
+  return p->precision == 32 ? x_pass<float>(p, f, p->grid, true) : x_pass<double>(p, f, p->grid, true);
+}
+int fused_forward_lines(nfft_plan* p) {
+  int rc;
+  if (p->precision == 32) {
+    rc = line_pass<float>(p, 1, true);
+    if (!rc && p->D == 3) rc = line_pass<float>(p, 2, true);
+  } else {
+    rc = line_pass<double>(p, 1, true);
+    if (!rc && p->D == 3) rc = line_pass<double>(p, 2, true);
+  }
+  return rc;
+}
+// adjoint: grid -> backward FFT lines (Z', Y'), then X' with crop + deconvolution
+int fused_adjoint_lines(nfft_plan* p) {
+  int rc = NFFT_OK;
+  if (p->precision == 32) {
+    if (p->D == 3) rc = line_pass<float>(p, 2, false);
+    if (!rc) rc = line_pass<float>(p, 1, false);
+  } else {
+    if (p->D == 3) rc = line_pass<double>(p, 2, false);
+    if (!rc) rc = line_pass<double>(p, 1, false);
+  }
+  return rc;
+}
+int fused_adjoint_x(nfft_plan* p, void* f) {
+  return p->precision == 32 ? x_pass<float>(p, p->grid, f, false) : x_pass<double>(p, p->grid, f, false);
+}
+
+}  // namespace nfft

@@ -105,6 +105,10 @@ struct nfft_plan {
   bool fft_ok = false, fft_tail_ok = false, fft_line_ok = false;
   int64_t slice_head = 0, slice_tail = 0, slice_size = 0;
   void* fft_work = nullptr;
+  // fused pruned FFT (fft.cu): used instead of pad + cuFFT / cuFFT + crop on
+  // the transform path when every Ntilde_d is a power of two in [64, 1024]
+  bool fused_fft = false;
+  void* fft_tw[3] = {};       // per dimension: exp(-2 pi i q / Ntilde_d), q < Ntilde_d (T complex)
   size_t real_size = 4;
 
   void* grid = nullptr;       // tmpVec, |Ntilde| complex
@@ -176,6 +180,12 @@ int launch_interp(const nfft_plan* p, const void* g, int g_real, void* fhat, int
 int launch_spread(nfft_plan* p, const void* fhat, int fhat_real, void* g, int g_real);
 // plan.cu: the grid FFT of a plan (pruned for D >= 2)
 int exec_fft_plan(nfft_plan* p, int dir);
+// fft.cu: fused pruned FFT with the deconvolution
+int fused_fft_init(nfft_plan* p);
+int fused_forward_x(nfft_plan* p, const void* f);
+int fused_forward_lines(nfft_plan* p);
+int fused_adjoint_lines(nfft_plan* p);
+int fused_adjoint_x(nfft_plan* p, void* f);
 // gradk.cu
 int launch_grad_nodes(const nfft_plan* p, const void* g, const void* w, void* dk);
 // plain.cu (per-node kernels of the plain path, blocking = 0)

@@ -520,6 +520,8 @@ int nfft_plan_create(nfft_plan** out, int precision, int D, const int64_t* N, in
   // cuFFT plans (Julia's column-major grid is C order with reversed dims)
   rc = make_fft_plans(p);
   if (rc) return fail(rc);
+  rc = fused_fft_init(p);
+  if (rc) return fail(rc);
   if (prm.timing) {
     p->timing_on = true;
     for (int s = 0; s < nfft_plan::kRing; ++s) {
@@ -548,6 +550,7 @@ int nfft_plan_destroy(nfft_plan* p) {
   if (p->fft_tail_ok) cufftDestroy(p->fft_tail);
   if (p->fft_line_ok) cufftDestroy(p->fft_line);
   cudaFree(p->fft_work);
+  for (int d = 0; d < 3; ++d) cudaFree(p->fft_tw[d]);
   if (p->timing_on)
     for (int s = 0; s < nfft_plan::kRing; ++s)
       for (int i = 0; i < 4; ++i) cudaEventDestroy(p->ev[s][i]);
@@ -686,10 +689,10 @@ int nfft_forward(nfft_plan* p, const void* f, void* fhat) {
   if (rc) return rc;
   const int slot = p->timing_on ? ring_slot(p) : 0;
   record(p, slot, 0);
-  rc = launch_pad_apodize(p, f, p->grid);
+  rc = p->fused_fft ? fused_forward_x(p, f) : launch_pad_apodize(p, f, p->grid);
   if (rc) return rc;
   record(p, slot, 1);
-  rc = exec_fft(p, CUFFT_FORWARD);
+  rc = p->fused_fft ? fused_forward_lines(p) : exec_fft(p, CUFFT_FORWARD);
   if (rc) return rc;
   record(p, slot, 2);
   rc = p->prm.blocking ? launch_interp(p, p->grid, 0, fhat, 0) : launch_plain_interp(p, p->grid, 0, fhat, 0);
@@ -707,10 +710,10 @@ int nfft_adjoint(nfft_plan* p, const void* fhat, void* f) {
   rc = p->prm.blocking ? launch_spread(p, fhat, 0, p->grid, 0) : launch_plain_spread(p, fhat, 0, p->grid, 0);
   if (rc) return rc;
   record(p, slot, 1);
-  rc = exec_fft(p, CUFFT_INVERSE);
+  rc = p->fused_fft ? fused_adjoint_lines(p) : exec_fft(p, CUFFT_INVERSE);
   if (rc) return rc;
   record(p, slot, 2);
-  rc = launch_crop_apodize(p, p->grid, f);
+  rc = p->fused_fft ? fused_adjoint_x(p, f) : launch_crop_apodize(p, p->grid, f);
   if (rc) return rc;
   record(p, slot, 3);
   finish_record(p, slot, 1);
@@ -784,9 +787,9 @@ int nfft_deconvolve_transpose(nfft_plan* p, const void* g, void* f) {
 int nfft_grad_nodes(nfft_plan* p, const void* v, const void* w, void* dk) {
   int rc = require_nodes(p);
   if (rc) return rc;
-  rc = launch_pad_apodize(p, v, p->grid);
+  rc = p->fused_fft ? fused_forward_x(p, v) : launch_pad_apodize(p, v, p->grid);
   if (rc) return rc;
-  rc = exec_fft(p, CUFFT_FORWARD);
+  rc = p->fused_fft ? fused_forward_lines(p) : exec_fft(p, CUFFT_FORWARD);
   if (rc) return rc;
   return launch_grad_nodes(p, p->grid, w, dk);
 }

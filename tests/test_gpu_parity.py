@@ -177,3 +177,46 @@ def test_pruned_fft_odd_and_even_sizes(D, N):
     y, x = gpu_fwd_adj(p, f, fhat)
     assert oracle.rel_l2(y, op.forward(f)) < TOL64
     assert oracle.rel_l2(colmajor_flat(x), colmajor_flat(op.adjoint(fhat))) < TOL64
+
+
+FUSED_CASES = [
+    # (N, sigma): every Ntilde_d a power of two in [64, 1024] -> fused pruned FFT path
+    ((64, 128), 2.0),
+    ((51, 26), 2.5),           # odd N: head 26 / tail 25 image rows; Ntilde (128, 64)
+    ((32, 64, 32), 2.0),
+    ((26, 51, 26), 2.5),       # Ntilde (64, 128, 64)
+]
+
+
+@pytest.mark.parametrize("N,sigma", FUSED_CASES)
+@pytest.mark.parametrize("prec", [64, 32])
+def test_fused_fft_matches_oracle_and_cufft(N, sigma, prec, monkeypatch):
+    """The fused pad/deconvolve + pruned FFT (and pruned inverse FFT + crop)
+    against the oracle and against the same plan on cuFFT."""
+    dtype = np.float64 if prec == 64 else np.float32
+    D = len(N)
+    M = 3000
+    k, f, fhat = rand_problem(D, N, M, seed=77 + D, dtype=dtype)
+    p = nf.plan_nfft(k, N, m=4, sigma=sigma, precompute=oracle.TENSOR)
+    assert all(n & (n - 1) == 0 for n in p.Ñ)
+    monkeypatch.setenv("NFFT_GB300_FFT", "cufft")
+    q = nf.plan_nfft(k, N, m=4, sigma=sigma, precompute=oracle.TENSOR)
+    monkeypatch.delenv("NFFT_GB300_FFT")
+    y, x = gpu_fwd_adj(p, f, fhat)
+    yq, xq = gpu_fwd_adj(q, f, fhat)
+    op = oracle.OraclePlan(k.astype(np.float64), N, m=4, sigma=sigma)
+    tol = TOL64 if prec == 64 else TOL32
+    assert oracle.rel_l2(y, op.forward(f)) < tol
+    assert oracle.rel_l2(colmajor_flat(x), colmajor_flat(op.adjoint(fhat))) < tol
+    tol_c = 1e-13 if prec == 64 else 2e-6
+    assert oracle.rel_l2(y, yq) < tol_c
+    assert oracle.rel_l2(colmajor_flat(x), colmajor_flat(xq)) < tol_c
+    # node gradient path (forward transform, then the derivative gather)
+    w = torch.as_tensor(fhat).to(p.cdtype).cuda()
+    fd = nf.as_colmajor(f, N, p.cdtype)
+
+    def dk(plan):
+        out = torch.empty((M, D), dtype=plan.dtype, device="cuda").t()
+        return plan.grad_nodes_(out, fd, w).cpu().numpy()
+
+    assert oracle.rel_l2(dk(p), dk(q)) < 100 * tol_c
