@@ -17,7 +17,8 @@
 // The grid ends up (forward) or is read (adjoint) exactly as the unpruned
 // transform of the zero-padded grid.  Each CTA transforms W lines held in a
 // shared-memory tile [position][line] (row pitch W+1: transfers along a line
-// and butterflies across lines are both free of bank conflicts) with
+// and butterflies across lines are both free of bank conflicts), loaded with
+// asynchronous copies (cp.async, the whole tile in flight at once), with
 // radix-8 Stockham passes (a final radix-2 or radix-4 pass for 128, 256,
 // 1024) computed in registers; twiddles come from a per-length table
 // exp(-2 pi i q / n) built on the host in FP64.  Unnormalised, forward sign
@@ -164,13 +165,24 @@ __device__ __forceinline__ void fft_lines(Cx<T>* buf, const Cx<T>* __restrict__ 
   }
 }
 
+// 8- or 16-byte asynchronous global -> shared copy (cp.async, sm_80+): a
+// tile's loads are all in flight at once, without register staging.
+template <typename C> __device__ __forceinline__ void cp_async_elem(C* smem, const C* gmem) {
+  const unsigned sa = static_cast<unsigned>(__cvta_generic_to_shared(smem));
+  if constexpr (sizeof(C) == 8)
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(sa), "l"(gmem) : "memory");
+  else
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+
 // Move the W x n tile elements q = threadIdx.x + i * kFftThreads through
-// registers in batches of up to 16: every load of a batch is issued before
+// registers in batches of up to 8: every load of a batch is issued before
 // its stores, so a thread keeps a batch of global (or shared) loads in flight
 // instead of one load-store round trip per element.
 template <typename C, int ITEMS, typename Load, typename Store>
 __device__ __forceinline__ void staged_copy(Load ld, Store st) {
-  constexpr int CH = ITEMS < 16 ? ITEMS : 16;
+  constexpr int CH = ITEMS < 8 ? ITEMS : 8;
   static_assert(ITEMS % CH == 0, "tile items per thread");
 #pragma unroll 1
   for (int c0 = 0; c0 < ITEMS; c0 += CH) {
@@ -182,9 +194,13 @@ __device__ __forceinline__ void staged_copy(Load ld, Store st) {
   }
 }
 
-// Two CTAs per SM (registers capped at 128) where the tile's registers fit
-// without spilling; one for the largest lines.
-template <typename T, int N> constexpr int fft_min_blocks() { return (sizeof(T) == 4 ? N <= 512 : N <= 256) ? 2 : 1; }
+// CTAs per SM the register allocation must allow: 3 for the forward FP32
+// kernels up to 512 (a few spilled bytes, measured faster), 2 for the
+// backward ones (whose spills at 3 cost more than the occupancy gains),
+// 1 for the largest lines.
+template <typename T, int N, bool FWD> constexpr int fft_min_blocks() {
+  return (sizeof(T) == 4 ? N <= 512 : N <= 256) ? ((sizeof(T) == 4 && FWD) ? 3 : 2) : 1;
+}
 
 struct FftGeom {
   int N[3], Nt[3];
@@ -197,7 +213,7 @@ template <typename T> struct Inv3 {
 
 // forward X: image rows -> deconvolved, zero-padded, transformed grid rows
 template <typename T, int NX, int W>
-__global__ void __launch_bounds__(kFftThreads, fft_min_blocks<T, NX>()) fft_x_pad_kernel(FftGeom G, Inv3<T> inv, const Cx<T>* __restrict__ f,
+__global__ void __launch_bounds__(kFftThreads, fft_min_blocks<T, NX, true>()) fft_x_pad_kernel(FftGeom G, Inv3<T> inv, const Cx<T>* __restrict__ f,
                                                                 Cx<T>* __restrict__ g, const Cx<T>* __restrict__ tw) {
   using C = Cx<T>;
   extern __shared__ __align__(16) unsigned char fft_smem[];
@@ -224,24 +240,37 @@ __global__ void __launch_bounds__(kFftThreads, fft_min_blocks<T, NX>()) fft_x_pa
     s_goff[threadIdx.x] = go;
   }
   __syncthreads();
-  staged_copy<C, ITEMS>(
-      [&](int q) {
-        const int pos = q % NX, w = q / NX;
-        const int nx = wrap_once(pos + h0, NX);
-        C v;
-        v.x = T(0);
-        v.y = T(0);
-        if (r0 + w < rows && nx < N0) v = f[nx + int64_t(N0) * (r0 + w)];
-        return v;
-      },
-      [&](int q, C v) {
-        const int pos = q % NX, w = q / NX;
-        const int nx = wrap_once(pos + h0, NX);
-        const T s = nx < N0 ? __ldg(inv.d[0] + nx) * s_row[w] : T(0);
-        v.x *= s;
-        v.y *= s;
-        buf[pos * P + w] = v;
-      });
+  // raw image values land asynchronously; padding positions are zeroed
+#pragma unroll 4
+  for (int i = 0; i < ITEMS; ++i) {
+    const int q = int(threadIdx.x) + i * kFftThreads;
+    const int pos = q % NX, w = q / NX;
+    const int nx = wrap_once(pos + h0, NX);
+    if (r0 + w < rows && nx < N0) {
+      cp_async_elem(buf + pos * P + w, f + nx + int64_t(N0) * (r0 + w));
+    } else {
+      C z;
+      z.x = T(0);
+      z.y = T(0);
+      buf[pos * P + w] = z;
+    }
+  }
+  cp_async_wait_all();
+  __syncthreads();
+  // deconvolution factors (each thread scales the elements it copied)
+#pragma unroll 4
+  for (int i = 0; i < ITEMS; ++i) {
+    const int q = int(threadIdx.x) + i * kFftThreads;
+    const int pos = q % NX, w = q / NX;
+    const int nx = wrap_once(pos + h0, NX);
+    if (nx < N0) {
+      const T sc = __ldg(inv.d[0] + nx) * s_row[w];
+      C v = buf[pos * P + w];
+      v.x *= sc;
+      v.y *= sc;
+      buf[pos * P + w] = v;
+    }
+  }
   __syncthreads();
   fft_lines<T, -1, NX, W>(buf, tw);
   staged_copy<C, ITEMS>([&](int q) { return buf[(q % NX) * P + q / NX]; },
@@ -252,7 +281,7 @@ __global__ void __launch_bounds__(kFftThreads, fft_min_blocks<T, NX>()) fft_x_pa
 
 // adjoint X': grid rows of the image -> transformed, cropped, deconvolved image rows
 template <typename T, int NX, int W>
-__global__ void __launch_bounds__(kFftThreads, fft_min_blocks<T, NX>()) fft_x_crop_kernel(FftGeom G, Inv3<T> inv, const Cx<T>* __restrict__ g,
+__global__ void __launch_bounds__(kFftThreads, fft_min_blocks<T, NX, false>()) fft_x_crop_kernel(FftGeom G, Inv3<T> inv, const Cx<T>* __restrict__ g,
                                                                  Cx<T>* __restrict__ f, const Cx<T>* __restrict__ tw) {
   using C = Cx<T>;
   extern __shared__ __align__(16) unsigned char fft_smem[];
@@ -278,15 +307,20 @@ __global__ void __launch_bounds__(kFftThreads, fft_min_blocks<T, NX>()) fft_x_cr
     s_goff[threadIdx.x] = go;
   }
   __syncthreads();
-  staged_copy<C, ITEMS>(
-      [&](int q) {
-        C v;
-        v.x = T(0);
-        v.y = T(0);
-        if (r0 + q / NX < rows) v = g[s_goff[q / NX] + q % NX];
-        return v;
-      },
-      [&](int q, C v) { buf[(q % NX) * P + q / NX] = v; });
+#pragma unroll 4
+  for (int i = 0; i < ITEMS; ++i) {
+    const int q = int(threadIdx.x) + i * kFftThreads;
+    const int pos = q % NX, w = q / NX;
+    if (r0 + w < rows) {
+      cp_async_elem(buf + pos * P + w, g + s_goff[w] + pos);
+    } else {
+      C z;
+      z.x = T(0);
+      z.y = T(0);
+      buf[pos * P + w] = z;
+    }
+  }
+  cp_async_wait_all();
   __syncthreads();
   fft_lines<T, 1, NX, W>(buf, tw);
   staged_copy<C, ITEMS>([&](int q) { return buf[(q % NX) * P + q / NX]; },
@@ -317,7 +351,7 @@ struct LineGeom {
 };
 
 template <typename T, int NL, int W, bool FWD>
-__global__ void __launch_bounds__(kFftThreads, fft_min_blocks<T, NL>()) fft_lines_kernel(LineGeom L, Cx<T>* __restrict__ g,
+__global__ void __launch_bounds__(kFftThreads, fft_min_blocks<T, NL, FWD>()) fft_lines_kernel(LineGeom L, Cx<T>* __restrict__ g,
                                                                 const Cx<T>* __restrict__ tw) {
   using C = Cx<T>;
   extern __shared__ __align__(16) unsigned char fft_smem[];
@@ -329,27 +363,38 @@ __global__ void __launch_bounds__(kFftThreads, fft_min_blocks<T, NL>()) fft_line
   C* base = g + int64_t(go) * L.outer_stride + int64_t(tile) * W;
   const int head = L.n_img - L.n_img / 2;   // image positions [0, head) and [NL - n_img/2, NL)
   const int tail0 = NL - L.n_img / 2;
-  constexpr int ITEMS = NL * W / kFftThreads;
-  staged_copy<C, ITEMS>(
-      [&](int q) {
-        const int w = q % W, pos = q / W;
-        C v;
-        v.x = T(0);
-        v.y = T(0);
-        if (!FWD || pos < head || pos >= tail0) v = base[int64_t(pos) * L.stride + w];
-        return v;
-      },
-      [&](int q, C v) { buf[(q / W) * P + q % W] = v; });
+  // thread -> fixed column w, positions p0, p0 + PS, ...
+  constexpr int PS = kFftThreads / W;
+  const int w = threadIdx.x % W, p0 = threadIdx.x / W;
+  const C* src = base + w + int64_t(p0) * L.stride;
+  const int64_t step = int64_t(PS) * L.stride;
+#pragma unroll 4
+  for (int pos = p0; pos < NL; pos += PS, src += step) {
+    if (!FWD || pos < head || pos >= tail0) {
+      cp_async_elem(buf + pos * P + w, src);
+    } else {
+      C z;
+      z.x = T(0);
+      z.y = T(0);
+      buf[pos * P + w] = z;
+    }
+  }
+  cp_async_wait_all();
   __syncthreads();
   fft_lines<T, FWD ? -1 : 1, NL, W>(buf, tw);
-  staged_copy<C, ITEMS>([&](int q) { return buf[(q / W) * P + q % W]; },
-                        [&](int q, C v) {
-                          const int pos = q / W;
-                          if (FWD || pos < head || pos >= tail0) base[int64_t(pos) * L.stride + q % W] = v;
-                        });
+  C* dst = base + w + int64_t(p0) * L.stride;
+#pragma unroll 4
+  for (int pos = p0; pos < NL; pos += PS, dst += step)
+    if (FWD || pos < head || pos >= tail0) *dst = buf[pos * P + w];
 }
 
-template <typename T> constexpr int lines_per_cta() { return sizeof(T) == 4 ? 16 : 8; }
+#ifndef NFFT_FFT_W32
+#define NFFT_FFT_W32 16
+#endif
+#ifndef NFFT_FFT_W64
+#define NFFT_FFT_W64 8
+#endif
+template <typename T> constexpr int lines_per_cta() { return sizeof(T) == 4 ? NFFT_FFT_W32 : NFFT_FFT_W64; }
 
 template <int NL, typename T> size_t fft_smem_bytes() {
   return size_t(NL) * (lines_per_cta<T>() + 1) * sizeof(Cx<T>);
