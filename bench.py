@@ -41,9 +41,13 @@ N3 = (256, 256, 256)
 SPOKES, SAMPLES = 8192, 512
 M_NODES = SPOKES * SAMPLES
 WORKLOAD = "3D radial koosh-ball NFFT fwd+adj, N=256^3, 8192 spokes x 512 samples (M=4194304), KB m=4 sigma=2"
-# DRAM bytes (read + write) per launch of the spreading kernel from one ncu
-# capture (profiles/spread_tile_radial256.md); None until measured.
-SPREAD_DRAM_BYTES = None
+# DRAM bytes (read + write) per launch of the spreading kernel on this
+# workload, from one ncu capture of the full-size launch
+# (profiles/spread_owned_radial256.md: 1.115 GB read + 0.564 GB write).
+SPREAD_DRAM_BYTES = 1.679e9
+# What bounds the dominant kernel on chip (same capture).
+SPREAD_LIMITER = ("shared-memory pipe 70.7% and instruction issue 80.8% of peak (ncu); the 20 B of shared-memory "
+                  "traffic per tap put the tap phase at 1.07 ms, HBM is not the limiter")
 
 
 def radial_nodes(dtype=np.float32):
@@ -364,18 +368,21 @@ def run_ours(args):
     alg = {
         "spread_ms": M_NODES * (D * s_r + s_c) + ng * s_c,
         "gather_ms": ng * s_c + M_NODES * (D * s_r + s_c),
-        "deconv_pad_ms": nimg * s_c + ng * s_c,
-        "crop_ms": 2 * nimg * s_c,
+        # fused x-line kernels: the image and the image rows of the grid (2 N0 x N1 x N2)
+        "deconv_pad_ms": nimg * s_c + 2 * nimg * s_c,
+        "crop_ms": 2 * nimg * s_c + nimg * s_c,
     }
     dom = max(alg, key=lambda s: stages[s])
     t_dom = stages[dom] * 1e-3
     achieved = alg[dom] / t_dom / 1e9
-    kernel_names = {"spread_ms": "spread_tile_kernel", "gather_ms": "interp_warp_kernel",
-                    "deconv_pad_ms": "pad_apodize_kernel", "crop_ms": "crop_apodize_kernel"}
+    kernel_names = {"spread_ms": "spread_owned_kernel (stage: grid memset + value sort + kernel)",
+                    "gather_ms": "interp_kernel", "deconv_pad_ms": "fft_x_pad_kernel",
+                    "crop_ms": "fft_x_crop_kernel"}
     roofline = {"bound": "hbm", "kernel": kernel_names[dom], "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "peak_source": f"{peak_kind} hbm_gbs",
                 "algorithmic_bytes": alg[dom],
-                "traffic": SPREAD_DRAM_BYTES if dom == "spread_ms" else None}
+                "traffic": SPREAD_DRAM_BYTES if dom == "spread_ms" else None,
+                "limiter": SPREAD_LIMITER if dom == "spread_ms" else None}
     pair_bytes = 7 * ng * s_c + 3 * nimg * s_c + 2 * M_NODES * (D * s_r + s_c)
     pair_gbs = pair_bytes / (t_dev / args.steps) / 1e9
 
