@@ -136,6 +136,8 @@ void default_block(nfft_plan* p) {
   // warps per CTA), 4096 (1-D); the last dimension halved in FP64.  The
   // reference's blockSize keyword overrides them.
   int64_t def[3][3] = {{4096, 1, 1}, {32, 32, 1}, {16, 16, 16}};
+  // compensated 1-D rows hold 16- or 32-byte accumulators and one warp each
+  if (p->prm.compensated) def[0][0] = 512;
   for (int d = 0; d < 3; ++d) {
     int64_t b = def[p->D - 1][d];
     if (p->precision == 64 && d == p->D - 1) b = b > 1 ? b / 2 : 1;

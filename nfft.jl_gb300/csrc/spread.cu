@@ -15,7 +15,9 @@
 //     ~17x the throughput of shared-memory float atomics on GB300), and can
 //     carry a Kahan compensation term (compensated = 1).  Nodes are staged in
 //     shared memory in batches (window values, x*y weight products, value);
-//   * D = 1 (spread_pad_kernel): 32/G nodes per warp, shared-memory atomics;
+//   * D = 1 (spread_pad1_kernel): 32/G nodes per warp, shared-memory atomics;
+//     compensated (spread_line_kahan_kernel): one warp per task, lane l owns
+//     the padded positions x = l mod 32, Kahan read-modify-writes;
 //   * the padded tile is added to the zeroed grid with vector global atomics
 //     (red.global.add.v2), wrapping periodically; all-zero points are skipped.
 // The lock of the reference becomes the L2 atomics of the flush.
@@ -43,6 +45,19 @@ int spread_launch(nfft_plan* p, const void* fhat, void* g) {
   const C* fp = static_cast<const C*>(fhat);
   T* gp = static_cast<T*>(g);
   if constexpr (D == 1) {
+    if (p->prm.compensated) {
+      const size_t smem = sizeof(typename Acc<T, true>::type) * size_t(p->bs[0] + L - 1);
+      if (smem > 227 * 1024) {
+        set_error("compensated spreading row of %zu bytes does not fit in shared memory; use a smaller blockSize",
+                  smem);
+        return NFFT_ERR_UNSUPPORTED;
+      }
+      auto kern = p->wtab ? spread_line_kahan_kernel<L, T, true> : spread_line_kahan_kernel<L, T, false>;
+      NFFT_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
+      kern<<<unsigned(p->n_tasks), 32, smem, p->stream>>>(G, Nd, p->tasks, fp, gp);
+      NFFT_LAUNCH_CHECK();
+      return NFFT_OK;
+    }
     const size_t smem = 2 * sizeof(T) * size_t(p->bs[0] + L - 1);
     if (smem > 227 * 1024) {
       set_error("spreading row of %zu bytes does not fit in shared memory; use a smaller blockSize", smem);

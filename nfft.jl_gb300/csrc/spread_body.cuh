@@ -69,7 +69,7 @@ __device__ __forceinline__ void flush_tile(const Geom<T>& G, const typename Acc<
   int r = rr < rpi ? warp * rpi + rr : rows;
   int y = r % P1, z = r / P1;
   for (; r < rows; r += step) {
-    const int gy = small ? wrap_any(o1 - m1 + y, G.Nt[1]) : wrap_once(o1 - m1 + y, G.Nt[1]);
+    const int gy = D >= 2 ? (small ? wrap_any(o1 - m1 + y, G.Nt[1]) : wrap_once(o1 - m1 + y, G.Nt[1])) : 0;
     const int gz = D == 3 ? (small ? wrap_any(o2 - m1 + z, G.Nt[2]) : wrap_once(o2 - m1 + z, G.Nt[2])) : 0;
     T* grow = g + 2 * (int64_t(gz) * G.plane + int64_t(gy) * Nt0);
     const auto* srow = acc + z * plane + y * pitch;
@@ -430,6 +430,70 @@ __global__ void __launch_bounds__(kSpreadThreads) spread_pad1_kernel(Geom<T> G, 
       red_add2<T>(g + 2 * int64_t(gx), a, bb);
     }
   }
+}
+
+// D = 1, compensated (compensated = 1): one warp per task; lane l owns the
+// padded positions x = l mod 32, so each of a node's L <= 16 taps has exactly
+// one owner lane and the Kahan read-modify-write needs no atomics.  Nodes are
+// visited in bin-sorted order (input order within a tile), the next node's
+// data loaded while the current one is added.
+template <int L, typename T, bool TABLE>
+__global__ void __launch_bounds__(32) spread_line_kahan_kernel(Geom<T> G, Nodes<T> Nd, const int4* __restrict__ tasks,
+                                                                const typename Cplx<T>::type* __restrict__ fhat,
+                                                                T* __restrict__ g) {
+  using C = typename Cplx<T>::type;
+  using A = typename Acc<T, true>::type;
+  constexpr int DEG = L + 1;
+  static_assert(L <= 32, "one owner lane per tap");
+  extern __shared__ __align__(32) unsigned char smem_raw[];
+  A* acc = reinterpret_cast<A*>(smem_raw);
+  const int4 task = tasks[blockIdx.x];
+  const int o0 = task.x * G.bs[0];
+  const int P0 = G.bs[0] + L - 1;
+  const int lane = threadIdx.x;
+  {
+    A zero;
+    memset(&zero, 0, sizeof(A));
+    for (int q = lane; q < P0; q += 32) acc[q] = zero;
+  }
+  __syncwarp();
+  auto load = [&](int i, int& x0, T& w, C& v) {
+    const int4 nd = __ldg(Nd.node4 + i);
+    x0 = nd.x - o0;
+    const int t = (lane - x0) & 31;
+    w = T(0);
+    if (t < L) {
+      if constexpr (TABLE) {
+        w = __ldg(Nd.wtab + int64_t(i) * L + t);
+      } else {
+        const T tt = __ldg(Nd.frac4 + 4 * int64_t(i)) - T(0.5);
+        const T* c = G.coeffs + t * DEG;
+        w = __ldg(c + DEG - 1);
+#pragma unroll
+        for (int q = DEG - 2; q >= 0; --q) w = fma(w, tt, __ldg(c + q));
+      }
+    }
+    v = __ldg(fhat + nd.w);
+  };
+  if (task.y < task.z) {
+    int x0;
+    T w;
+    C v;
+    load(task.y, x0, w, v);
+    for (int i = task.y; i < task.z; ++i) {
+      int x0n = 0;
+      T wn = T(0);
+      C vn = v;
+      if (i + 1 < task.z) load(i + 1, x0n, wn, vn);
+      const int t = (lane - x0) & 31;
+      if (t < L) kahan_add<A, T>(acc[x0 + t], w * v.x, w * v.y);
+      x0 = x0n;
+      w = wn;
+      v = vn;
+    }
+  }
+  __syncwarp();
+  flush_tile<1, T, true, 1>(G, acc, g, o0, 0, 0, P0, 1, 1, P0);
 }
 
 template <int D, int L, typename T>
