@@ -33,7 +33,13 @@
 namespace nfft {
 namespace {
 
-constexpr int kFftThreads = 256;
+#ifndef NFFT_FFT_FOURSTEP
+#define NFFT_FFT_FOURSTEP 1
+#endif
+#ifndef NFFT_FFT_THREADS
+#define NFFT_FFT_THREADS 256
+#endif
+constexpr int kFftThreads = NFFT_FFT_THREADS;
 
 template <typename T> using Cx = typename Cplx<T>::type;
 
@@ -199,6 +205,7 @@ __device__ __forceinline__ void staged_copy(Load ld, Store st) {
 // backward ones (whose spills at 3 cost more than the occupancy gains),
 // 1 for the largest lines.
 template <typename T, int N, bool FWD> constexpr int fft_min_blocks() {
+  if (kFftThreads > 256) return 1;
   return (sizeof(T) == 4 ? N <= 512 : N <= 256) ? ((sizeof(T) == 4 && FWD) ? 3 : 2) : 1;
 }
 
@@ -400,6 +407,235 @@ template <int NL, typename T> size_t fft_smem_bytes() {
   return size_t(NL) * (lines_per_cta<T>() + 1) * sizeof(Cx<T>);
 }
 
+
+// ---------------------------------------------------------------------------
+// FP32 lines of length N <= 512: four-step FFT in registers.  N = R1 R2;
+// pass 1 loads the R1 points n = R2 n1 + n2 of a line straight from global
+// memory into registers, transforms them (DFT of length R1), applies the
+// twiddles exp(S 2 pi i n2 k1 / N) and writes them to shared memory; pass 2
+// reads the R2 values of one k1, transforms them (DFT of length R2) and
+// writes X[k1 + R1 k2] straight to global memory.  A point crosses shared
+// memory once (16 bytes of shared traffic against 64 for the Stockham
+// passes), which keeps the kernel on the HBM side of its bounds.
+
+// cos(2 pi j / 32)
+__host__ __device__ constexpr double cos32(int j) {
+  switch (j & 31) {
+    case 0: return 1.0;
+    case 1: case 31: return 0.9807852804032304491261822;
+    case 2: case 30: return 0.9238795325112867561281832;
+    case 3: case 29: return 0.8314696123025452370787884;
+    case 4: case 28: return 0.7071067811865475244008444;
+    case 5: case 27: return 0.5555702330196022247428308;
+    case 6: case 26: return 0.3826834323650897717284600;
+    case 7: case 25: return 0.1950903220161282678482849;
+    case 8: case 24: return 0.0;
+    case 9: case 23: return -0.1950903220161282678482849;
+    case 10: case 22: return -0.3826834323650897717284600;
+    case 11: case 21: return -0.5555702330196022247428308;
+    case 12: case 20: return -0.7071067811865475244008444;
+    case 13: case 19: return -0.8314696123025452370787884;
+    case 14: case 18: return -0.9238795325112867561281832;
+    case 15: case 17: return -0.9807852804032304491261822;
+    default: return -1.0;  // 16
+  }
+}
+
+// In-register DFT of length R (2..32), natural order, kernel exp(S 2 pi i t q / R):
+// radix 2/4/8 directly, 16 and 32 by an even/odd split.
+template <int S, int R, typename C> __device__ __forceinline__ void dft_reg(C (&v)[R]) {
+  using T = decltype(v[0].x);
+  if constexpr (R <= 8) {
+    dft<S, R>(v);
+  } else {
+    C e[R / 2], o[R / 2];
+#pragma unroll
+    for (int t = 0; t < R / 2; ++t) {
+      e[t] = v[2 * t];
+      o[t] = v[2 * t + 1];
+    }
+    dft_reg<S, R / 2>(e);
+    dft_reg<S, R / 2>(o);
+#pragma unroll
+    for (int k = 0; k < R / 2; ++k) {
+      const int j = k * (32 / R);
+      const T c = T(cos32(j)), sn = T(S) * T(cos32(j - 8));
+      C t;
+      t.x = o[k].x * c - o[k].y * sn;
+      t.y = o[k].x * sn + o[k].y * c;
+      v[k] = c_add(e[k], t);
+      v[k + R / 2] = c_sub(e[k], t);
+    }
+  }
+}
+
+template <int N> struct Split4 {
+  static constexpr int R1 = N == 64 ? 8 : N == 128 ? 8 : N == 256 ? 16 : 16;
+  static constexpr int R2 = N / R1;
+};
+
+// v[k1] *= exp(S 2 pi i n2 k1 / N) for k1 >= 1 (table of exp(-2 pi i q / N))
+template <int S, int N, int R1, typename C>
+__device__ __forceinline__ void twiddle4(C (&v)[R1], int n2, const C* __restrict__ tw) {
+  if (n2 == 0) return;
+#pragma unroll
+  for (int k1 = 1; k1 < R1; ++k1) {
+    C tt = __ldg(tw + ((n2 * k1) & (N - 1)));
+    if constexpr (S > 0) tt.y = -tt.y;
+    v[k1] = c_mul(v[k1], tt);
+  }
+}
+
+constexpr int kW4 = 16;  // lines per CTA
+
+template <int NL, bool FWD>
+__global__ void __launch_bounds__(256, FWD ? 3 : 2) fft4_lines_kernel(LineGeom L, float2* __restrict__ g,
+                                                                      const float2* __restrict__ tw) {
+  using C = float2;
+  constexpr int R1 = Split4<NL>::R1, R2 = Split4<NL>::R2, W = kW4, P = W + 1, S = FWD ? -1 : 1;
+  extern __shared__ __align__(16) unsigned char fft_smem[];
+  C* y = reinterpret_cast<C*>(fft_smem);
+  const int tile = blockIdx.x % L.tiles_x;
+  const int o = blockIdx.x / L.tiles_x;
+  const int go = L.outer_N > 0 ? wrap_once(o - L.outer_N / 2, L.outer_Nt) : o;
+  C* base = g + int64_t(go) * L.outer_stride + int64_t(tile) * W;
+  const int head = L.n_img - L.n_img / 2, tail0 = NL - L.n_img / 2;
+  constexpr int T1 = W * R2, B1 = (T1 + 255) / 256;
+#pragma unroll
+  for (int b = 0; b < B1; ++b) {
+    const int task = int(threadIdx.x) + b * 256;
+    if (T1 % 256 == 0 || task < T1) {
+      const int w = task % W, n2 = task / W;
+      C v[R1];
+#pragma unroll
+      for (int n1 = 0; n1 < R1; ++n1) {
+        const int n = R2 * n1 + n2;
+        v[n1].x = 0.f;
+        v[n1].y = 0.f;
+        if (!FWD || n < head || n >= tail0) v[n1] = base[w + int64_t(n) * L.stride];
+      }
+      dft_reg<S, R1>(v);
+      twiddle4<S, NL, R1>(v, n2, tw);
+#pragma unroll
+      for (int k1 = 0; k1 < R1; ++k1) y[(n2 * R1 + k1) * P + w] = v[k1];
+    }
+  }
+  __syncthreads();
+  constexpr int T2 = W * R1, B2 = (T2 + 255) / 256;
+#pragma unroll
+  for (int b = 0; b < B2; ++b) {
+    const int task = int(threadIdx.x) + b * 256;
+    if (T2 % 256 == 0 || task < T2) {
+      const int w = task % W, k1 = task / W;
+      C v[R2];
+#pragma unroll
+      for (int n2 = 0; n2 < R2; ++n2) v[n2] = y[(n2 * R1 + k1) * P + w];
+      dft_reg<S, R2>(v);
+#pragma unroll
+      for (int k2 = 0; k2 < R2; ++k2) {
+        const int pos = k1 + R1 * k2;
+        if (FWD || pos < head || pos >= tail0) base[w + int64_t(pos) * L.stride] = v[k2];
+      }
+    }
+  }
+}
+
+// x lines of the image rows: forward pad + deconvolution + FFT (FWD), or
+// backward FFT + crop + deconvolution.
+template <int NX, bool FWD>
+__global__ void __launch_bounds__(256, FWD ? 3 : 2) fft4_x_kernel(FftGeom G, Inv3<float> inv,
+                                                                  const float2* __restrict__ src,
+                                                                  float2* __restrict__ dst,
+                                                                  const float2* __restrict__ tw) {
+  using C = float2;
+  constexpr int R1 = Split4<NX>::R1, R2 = Split4<NX>::R2, W = kW4, PR = R1 + 1, PW = R2 * PR, S = FWD ? -1 : 1;
+  extern __shared__ __align__(16) unsigned char fft_smem[];
+  C* y = reinterpret_cast<C*>(fft_smem);
+  __shared__ float s_row[W];
+  __shared__ int64_t s_goff[W];
+  const int64_t rows = int64_t(G.N[1]) * G.N[2];
+  const int64_t r0 = int64_t(blockIdx.x) * W;
+  const int N0 = G.N[0], h0 = G.N[0] / 2;
+  if (threadIdx.x < W) {
+    const int64_t r = r0 + threadIdx.x;
+    float sc = 0.f;
+    int64_t goff = 0;
+    if (r < rows) {
+      const int yy = int(r % G.N[1]), zz = int(r / G.N[1]);
+      sc = __ldg(inv.d[1] + yy) * __ldg(inv.d[2] + zz);
+      goff = int64_t(NX) * (wrap_once(yy - G.N[1] / 2, G.Nt[1]) +
+                            int64_t(G.Nt[1]) * wrap_once(zz - G.N[2] / 2, G.Nt[2]));
+    }
+    s_row[threadIdx.x] = sc;
+    s_goff[threadIdx.x] = goff;
+  }
+  __syncthreads();
+  constexpr int T1 = W * R2, B1 = (T1 + 255) / 256;
+#pragma unroll
+  for (int b = 0; b < B1; ++b) {
+    const int task = int(threadIdx.x) + b * 256;
+    if (T1 % 256 == 0 || task < T1) {
+      const int n2 = task % R2, w = task / R2;
+      const bool live = r0 + w < rows;
+      C v[R1];
+#pragma unroll
+      for (int n1 = 0; n1 < R1; ++n1) {
+        const int n = R2 * n1 + n2;
+        v[n1].x = 0.f;
+        v[n1].y = 0.f;
+        if (FWD) {
+          const int nx = wrap_once(n + h0, NX);
+          if (live && nx < N0) {
+            const C a = src[nx + int64_t(N0) * (r0 + w)];
+            const float sc = __ldg(inv.d[0] + nx) * s_row[w];
+            v[n1].x = a.x * sc;
+            v[n1].y = a.y * sc;
+          }
+        } else if (live) {
+          v[n1] = src[s_goff[w] + n];
+        }
+      }
+      dft_reg<S, R1>(v);
+      twiddle4<S, NX, R1>(v, n2, tw);
+#pragma unroll
+      for (int k1 = 0; k1 < R1; ++k1) y[w * PW + n2 * PR + k1] = v[k1];
+    }
+  }
+  __syncthreads();
+  constexpr int T2 = W * R1, B2 = (T2 + 255) / 256;
+#pragma unroll
+  for (int b = 0; b < B2; ++b) {
+    const int task = int(threadIdx.x) + b * 256;
+    if (T2 % 256 == 0 || task < T2) {
+      const int k1 = task % R1, w = task / R1;
+      if (r0 + w < rows) {
+        C v[R2];
+#pragma unroll
+        for (int n2 = 0; n2 < R2; ++n2) v[n2] = y[w * PW + n2 * PR + k1];
+        dft_reg<S, R2>(v);
+#pragma unroll
+        for (int k2 = 0; k2 < R2; ++k2) {
+          const int pos = k1 + R1 * k2;
+          if (FWD) {
+            dst[s_goff[w] + pos] = v[k2];
+          } else {
+            const int nx = wrap_once(pos + h0, NX);
+            if (nx < N0) {
+              const float sc = __ldg(inv.d[0] + nx) * s_row[w];
+              C out;
+              out.x = v[k2].x * sc;
+              out.y = v[k2].y * sc;
+              dst[nx + int64_t(N0) * (r0 + w)] = out;
+            }
+          }
+        }
+      }
+    }
+  }
+}
+
+template <int N> size_t fft4_smem_bytes() { return size_t(N) * (kW4 + 1) * sizeof(float2); }
+
 FftGeom make_fft_geom(const nfft_plan* p) {
   FftGeom G{};
   for (int d = 0; d < 3; ++d) {
@@ -427,6 +663,17 @@ template <typename K> int set_smem(K kern, size_t bytes) {
 
 template <typename T, int NX> int x_pass_t(nfft_plan* p, const void* src, void* dst, bool fwd) {
   using C = Cx<T>;
+  if constexpr (sizeof(T) == 4 && NX <= 512 && NFFT_FFT_FOURSTEP) {
+    const size_t smem = size_t(kW4) * Split4<NX>::R2 * (Split4<NX>::R1 + 1) * sizeof(float2);
+    const unsigned blocks = unsigned((p->N[1] * p->N[2] + kW4 - 1) / kW4);
+    const float2* tw = static_cast<const float2*>(p->fft_tw[0]);
+    auto kern = fwd ? fft4_x_kernel<NX, true> : fft4_x_kernel<NX, false>;
+    if (int rc = set_smem(kern, smem)) return rc;
+    kern<<<blocks, 256, smem, p->stream>>>(make_fft_geom(p), make_inv3<float>(p), static_cast<const float2*>(src),
+                                           static_cast<float2*>(dst), tw);
+    NFFT_LAUNCH_CHECK();
+    return NFFT_OK;
+  }
   constexpr int W = lines_per_cta<T>();
   const size_t smem = fft_smem_bytes<NX, T>();
   const int64_t rows = p->N[1] * p->N[2];
@@ -468,9 +715,19 @@ template <typename T, int NL> int line_pass_t(nfft_plan* p, int axis, bool fwd) 
     L.outer_Nt = int(p->Nt[1]);
     outer_count = p->Nt[1];
   }
-  const unsigned blocks = unsigned(outer_count * L.tiles_x);
   const C* tw = static_cast<const C*>(p->fft_tw[axis]);
   C* g = static_cast<C*>(p->grid);
+  if constexpr (sizeof(T) == 4 && NL <= 512 && NFFT_FFT_FOURSTEP) {
+    L.tiles_x = int(p->Nt[0] / kW4);
+    const unsigned blocks4 = unsigned(outer_count * L.tiles_x);
+    const size_t smem4 = fft4_smem_bytes<NL>();
+    auto kern = fwd ? fft4_lines_kernel<NL, true> : fft4_lines_kernel<NL, false>;
+    if (int rc = set_smem(kern, smem4)) return rc;
+    kern<<<blocks4, 256, smem4, p->stream>>>(L, g, tw);
+    NFFT_LAUNCH_CHECK();
+    return NFFT_OK;
+  }
+  const unsigned blocks = unsigned(outer_count * L.tiles_x);
   if (fwd) {
     auto kern = fft_lines_kernel<T, NL, W, true>;
     if (int rc = set_smem(kern, smem)) return rc;
