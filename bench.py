@@ -136,19 +136,50 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
+def ndft_forward_subset(k64, f, sub):
+    """Direct NDFT (src/direct.jl:99-123) in FP64 at the nodes `sub`:
+    fHat_j = sum_n f[n] exp(-2 pi i k_j . (n - N/2)), separable per node."""
+    N = f.shape
+    fc = np.asarray(f, np.complex128)
+    out = np.empty(len(sub), np.complex128)
+    for i, j in enumerate(sub):
+        t = fc
+        for d in reversed(range(len(N))):  # contract the last axis first
+            e = np.exp(-2j * np.pi * k64[d, j] * (np.arange(N[d]) - N[d] // 2))
+            t = t @ e if t.ndim > 1 else t.dot(e)
+        out[i] = t
+    return out
+
+
+def ndft_adjoint_subset(k64, N, fhat, lin):
+    """Direct adjoint NDFT (src/direct.jl:126-151) in FP64 at the column-major
+    linear output indices `lin`."""
+    fh = np.asarray(fhat, np.complex128)
+    out = np.empty(len(lin), np.complex128)
+    for i, q in enumerate(lin):
+        ph = np.zeros(k64.shape[1])
+        for d, n_d in enumerate(np.unravel_index(int(q), N, order="F")):
+            ph += k64[d] * (n_d - N[d] // 2)
+        out[i] = np.sum(fh * np.exp(2j * np.pi * ph))
+    return out
+
+
+def rel_l2(x, ref):
+    x = np.asarray(x).astype(np.complex128).ravel()
+    ref = np.asarray(ref).astype(np.complex128).ravel()
+    return float(np.linalg.norm(x - ref) / np.linalg.norm(ref))
+
+
 def rel_err_subset(k64, f, fhat, y, x, n_fwd=48, n_adj=24, seed=7):
     """Relative l2 errors of the GPU outputs on node / frequency subsets
-    against the FP64 NDFT (oracle)."""
-    from oracle import oracle
+    against the FP64 NDFT."""
     rng = np.random.default_rng(seed)
     M = k64.shape[1]
     sub = rng.choice(M, n_fwd, replace=False)
-    ref_y = oracle.ndft_forward(k64, f, subset=sub)
-    e_fwd = oracle.rel_l2(y[sub], ref_y)
+    e_fwd = rel_l2(y[sub], ndft_forward_subset(k64, f, sub))
     N = f.shape
     lin = rng.choice(int(np.prod(N)), n_adj, replace=False)
-    ref_x = oracle.ndft_adjoint(k64, N, fhat, subset=lin)
-    e_adj = oracle.rel_l2(x.ravel(order="F")[lin], ref_x)
+    e_adj = rel_l2(x.ravel(order="F")[lin], ndft_adjoint_subset(k64, N, fhat, lin))
     return e_fwd, e_adj
 
 
@@ -419,6 +450,201 @@ def run_ours(args):
     return 0
 
 
+class SparseBPath:
+    """The reference's GPU algorithm restated on this GPU with library calls
+    (ext/NFFTGPUArraysExt/implementation.jl:21-136): the |Ntilde| x M sparse
+    matrix B of exact window values built once (FULL precompute,
+    src/precomputation.jl:81-120, Int32 indices), forward = deconvolve into the
+    zero-padded grid + FFT + B^T g, adjoint = B fHat + backward FFT + crop.
+    B is a torch CSR matrix (cuSPARSE SpMM on [re, im] columns), the FFT is
+    torch.fft (cuFFT), the deconvolution factors are the plan's own.  It is
+    the plain-path comparator where B fits (nnz < 2^31)."""
+
+    def __init__(self, k, N, m, sigma, inv, real_dtype, device):
+        import warnings
+        import torch
+        warnings.filterwarnings("ignore", message="Sparse CSR tensor support is in beta")
+        self.torch = torch
+        D = len(N)
+        Nt = tuple(2 * (int(np.ceil(sigma * n)) // 2) for n in N)
+        self.N, self.Nt = tuple(N), Nt
+        ng = int(np.prod(Nt))
+        kk = torch.as_tensor(np.asarray(k, np.float64), device=device)
+        M = kk.shape[1]
+        L = 2 * m
+        b = math.pi * (2.0 - 1.0 / sigma)
+        idx = torch.zeros((M, 1), dtype=torch.int64, device=device)
+        w = torch.ones((M, 1), dtype=torch.float64, device=device)
+        stride = 1
+        for d in range(D):
+            xs = kk[d] * Nt[d]
+            c = torch.floor(xs)
+            t = c[:, None] - m + 1 + torch.arange(L, device=device, dtype=torch.float64)[None, :]
+            x = (xs[:, None] - t).abs()
+            r = torch.sqrt(torch.clamp(m * m - x * x, min=0.0))
+            wd = torch.where(x < m, torch.sinh(b * r) / (math.pi * torch.where(r > 0, r, torch.ones_like(r))),
+                             torch.zeros_like(x))
+            wd = torch.where(x == m, torch.full_like(x, b / math.pi), wd)
+            id_d = torch.remainder(t.to(torch.int64), Nt[d]) * stride
+            idx = (idx[:, :, None] + id_d[:, None, :]).reshape(M, -1)
+            w = (w[:, :, None] * wd[:, None, :]).reshape(M, -1)
+            stride *= Nt[d]
+        T = idx.shape[1]
+        rows = torch.arange(M, device=device, dtype=torch.int64).repeat_interleave(T)
+        vals = w.reshape(-1).to(real_dtype)
+        self.BT = torch.sparse_coo_tensor(torch.stack([rows, idx.reshape(-1)]), vals, (M, ng)).coalesce() \
+            .to_sparse_csr()
+        self.B = torch.sparse_coo_tensor(torch.stack([idx.reshape(-1), rows]), vals, (ng, M)).coalesce() \
+            .to_sparse_csr()
+        del idx, w, rows, vals
+        # image -> grid index and separable deconvolution factor (column-major)
+        gidx = torch.zeros(1, dtype=torch.int64, device=device)
+        fac = torch.ones(1, dtype=torch.float64, device=device)
+        gstride = 1
+        off = 0
+        for d in range(D):
+            n = torch.arange(N[d], device=device)
+            gd = torch.remainder(n - N[d] // 2, Nt[d]) * gstride
+            fd = torch.as_tensor(np.asarray(inv[off:off + N[d]], np.float64), device=device)
+            gidx = (gidx[None, :] + gd[:, None]).reshape(-1)
+            fac = (fac[None, :] * fd[:, None]).reshape(-1)
+            gstride *= Nt[d]
+            off += N[d]
+        self.gidx = gidx
+        self.fac = fac.to(real_dtype)
+        self.cdtype = torch.complex64 if real_dtype == torch.float32 else torch.complex128
+        self.ng = ng
+
+    def forward(self, f_flat):
+        torch = self.torch
+        g = torch.zeros(self.ng, dtype=self.cdtype, device=f_flat.device)
+        g[self.gidx] = f_flat * self.fac
+        G = torch.fft.fftn(g.view(self.Nt[::-1])).reshape(-1)
+        return torch.view_as_complex((self.BT @ torch.view_as_real(G)).contiguous())
+
+    def adjoint(self, fhat):
+        torch = self.torch
+        g = torch.view_as_complex((self.B @ torch.view_as_real(fhat)).contiguous())
+        G = torch.fft.ifftn(g.view(self.Nt[::-1]), norm="forward").reshape(-1)
+        return G[self.gidx] * self.fac
+
+
+def spiral_nodes(N, interleaves=32, samples=2048, turns=4.0):
+    """Archimedean spiral: r = 0.5 t, theta = 2 pi turns t + 2 pi i / interleaves."""
+    t = np.arange(samples) / samples
+    out = []
+    for i in range(interleaves):
+        th = 2 * np.pi * turns * t + 2 * np.pi * i / interleaves
+        out.append(np.stack([0.5 * t * np.cos(th), 0.5 * t * np.sin(th)]))
+    return np.clip(np.concatenate(out, axis=1), -0.5, 0.4999999)
+
+
+CONFIGS = {
+    "plain2d": dict(N=(128, 128), M=16384, m=4, prec=64, nodes="uniform", compensated=False,
+                    desc="2-D plain NFFT fwd+adj, N=128^2, M=16384 uniform, KB m=4 sigma=2, TENSOR, FP64"),
+    "line1d": dict(N=(1 << 22,), M=1 << 24, m=5, prec=32, nodes="uniform", compensated=True,
+                   desc="1-D NFFT fwd+adj, N=2^22, M=2^24 uniform, KB m=5 sigma=2, TENSOR, FP32, compensated"),
+    "spiral2d": dict(N=(256, 256), M=65536, m=4, prec=32, nodes="spiral", compensated=False,
+                     desc="2-D spiral (32 x 2048) fwd+adj+node gradient, N=256^2, KB m=4 sigma=2, FP32"),
+}
+
+
+def run_config(args):
+    """--workload plain2d | line1d | spiral2d: the other configurations,
+    measured as extra lines (ours, the sparse-B GPU comparator where B fits,
+    the oracle on the host cores)."""
+    import torch
+    import nfftgb300 as nf
+    cfg = CONFIGS[args.workload]
+    dev = torch.device("cuda", torch.cuda.current_device())
+    N, M, m = cfg["N"], cfg["M"], cfg["m"]
+    rdt = np.float32 if cfg["prec"] == 32 else np.float64
+    cd = torch.complex64 if cfg["prec"] == 32 else torch.complex128
+    rng = np.random.default_rng(123)
+    k = spiral_nodes(N[0]) if cfg["nodes"] == "spiral" else rng.random((len(N), M)) - 0.5
+    k = k.astype(rdt)
+    M = k.shape[1]
+    f_h = complex_normal(rng, N, np.complex128)
+    fh_h = complex_normal(rng, M, np.complex128)
+    p = nf.plan_nfft(k, N, m=m, sigma=2.0, precompute=nf.TENSOR, compensated=cfg["compensated"])
+    if args.autotune:
+        p.autotune(use_cache=True)
+    f = nf.as_colmajor(f_h, N, cd, dev)
+    fh = torch.as_tensor(fh_h).to(device=dev, dtype=cd)
+    y = torch.empty(M, dtype=cd, device=dev)
+    x = nf.empty_image(N, cd, dev)
+    grad = args.workload == "spiral2d"
+    dk = torch.empty((M, len(N)), dtype=p.dtype, device=dev).t() if grad else None
+
+    def step():
+        p.forward_(y, f)
+        p.adjoint_(x, fh)
+        if grad:
+            p.grad_nodes_(dk, f, fh)
+
+    def timed(fn, steps, warmup):
+        for _ in range(warmup):
+            fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(steps):
+            fn()
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) * 1e-3 / steps
+
+    l0 = nf.kernel_launch_count()
+    t_ours = timed(step, args.steps, args.warmup)
+    launches = (nf.kernel_launch_count() - l0) // (args.steps + args.warmup)
+    yo, xo = y.cpu().numpy(), x.cpu().numpy()
+    rs = np.random.default_rng(7)
+    sub = rs.choice(M, min(M, 48), replace=False)
+    lin = rs.choice(int(np.prod(N)), 24, replace=False)
+    k64 = k.astype(np.float64)
+    err = {"forward": rel_l2(yo[sub], ndft_forward_subset(k64, f_h, sub)),
+           "adjoint": rel_l2(xo.ravel(order="F")[lin], ndft_adjoint_subset(k64, N, fh_h, lin))}
+    line = {"metric": f"{args.workload}: fwd+adj{'+dk' if grad else ''} NFFT nodes/s", "value": M / t_ours,
+            "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": t_ours * 1e3, "higher_is_better": True, "dtype": "f32" if cfg["prec"] == 32 else "f64",
+            "data": "synthetic", "config": {"workload": cfg["desc"], "block_size": list(p.params.blockSize)},
+            "gpu_launches_per_step": launches, "rel_err_vs_fp64_ndft": err}
+    # the reference's GPU algorithm (sparse B), where it fits
+    if not args.no_plain and M * (2 * m) ** len(N) < 2 ** 31:
+        inv = np.concatenate([p.deconv_factors()[d] for d in range(len(N))])
+        sb = SparseBPath(k, N, m, 2.0, inv, p.dtype, dev)
+        f_flat = f.permute(*reversed(range(len(N)))).reshape(-1).contiguous()
+        t_sb = timed(lambda: (sb.forward(f_flat), sb.adjoint(fh)), args.steps, args.warmup)
+        ys = sb.forward(f_flat).cpu().numpy()
+        line["sparse_b_gpu"] = {"value": M / t_sb, "unit": UNIT, "ms_per_step": t_sb * 1e3,
+                                "speedup_of_value": t_sb / t_ours, "nnz": int(sb.BT._nnz()),
+                                "rel_diff_forward_vs_ours": rel_l2(ys, yo),
+                                "what": "reference GPU algorithm restated: FULL sparse B (cuSPARSE SpMM via torch) + "
+                                        "cuFFT (torch.fft) + deconvolution; fwd+adj only"}
+        del sb
+        torch.cuda.empty_cache()
+    if not args.no_cpu_baseline:
+        from oracle import oracle
+        lib = oracle.lib()
+        threads = lib.oracle_num_threads()
+        op = oracle.OraclePlan(k, N, m=m, sigma=2.0, precompute=oracle.TENSOR, dtype=rdt, fft_workers=threads)
+        fr, fhr = f_h.astype(np.complex128 if rdt == np.float64 else np.complex64), fh_h.astype(
+            np.complex128 if rdt == np.float64 else np.complex64)
+        times = []
+        t_start = time.perf_counter()
+        while len(times) < 5 and time.perf_counter() - t_start < 60:
+            t0 = time.perf_counter()
+            op.forward(fr)
+            op.adjoint(fhr)
+            times.append(time.perf_counter() - t0)
+        per = statistics.median(times)
+        line["cpu_baseline"] = {"value": M / per, "unit": UNIT, "cores": threads, "kind": "port",
+                                "sample": f"full workload, {len(times)} fwd+adj pairs (no dk); oracle restatement "
+                                          f"of NFFT.jl blocked TENSOR, scipy.fft workers={threads}"}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def batched_plans(seed=4, nplans=64):
     """64 2-D FP32 plans: N_i from {64, 96, 128, 192, 256, 384, 512} (grids of
     2 N_i, radix-3 sizes included), M_i = floor(10^U(4, 6)), nodes U[-1/2, 1/2)^2."""
@@ -505,11 +731,14 @@ def main():
     ap.add_argument("--small", action="store_true",
                     help="profiling case of the same kernels: N=128^3, 2048 spokes x 256 samples (same node "
                          "density; 134 MB grid, above L2) -- not a bench line")
-    ap.add_argument("--workload", default="radial3d", choices=["radial3d", "batched2d"],
-                    help="radial3d: the headline line; batched2d: the 64 batched 2-D plans (extra measurement)")
+    ap.add_argument("--workload", default="radial3d",
+                    choices=["radial3d", "batched2d", "plain2d", "line1d", "spiral2d"],
+                    help="radial3d: the headline line; the others print extra lines for the other configurations")
     args = ap.parse_args()
     if args.workload == "batched2d":
         return run_batched(args)
+    if args.workload in CONFIGS:
+        return run_config(args)
     if args.small:
         global N3, SPOKES, SAMPLES, M_NODES, WORKLOAD
         N3, SPOKES, SAMPLES = (128, 128, 128), 2048, 256

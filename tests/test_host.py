@@ -32,3 +32,37 @@ def test_exceptions_are_julia_named():
     assert issubclass(nf.DimensionMismatch, ValueError)
     assert issubclass(nf.ArgumentError, ValueError)
     assert int(nf.PrecomputeFlags.FULL) == 1 and int(nf.PrecomputeFlags.POLYNOMIAL) == 4
+
+
+@pytest.mark.parametrize("N", [(16,), (12, 10), (8, 6, 10)])
+def test_bench_sparse_b_comparator_matches_oracle(N):
+    """bench.py's restatement of the reference's GPU algorithm (sparse B of
+    exact window values + FFT) equals the oracle's FULL plan (on the CPU)."""
+    torch = pytest.importorskip("torch")
+    import bench
+    from oracle import oracle
+    rng = np.random.default_rng(len(N))
+    D, M = len(N), 300
+    k = rng.random((D, M)) - 0.5
+    f = rng.standard_normal(N) + 1j * rng.standard_normal(N)
+    fh = rng.standard_normal(M) + 1j * rng.standard_normal(M)
+    inv = np.concatenate(oracle.deconv_factors("kaiser_bessel", N, tuple(2 * n for n in N), 4, 2.0))
+    sb = bench.SparseBPath(k, N, 4, 2.0, inv, torch.float64, "cpu")
+    y = sb.forward(torch.as_tensor(f.ravel(order="F"))).numpy()
+    x = sb.adjoint(torch.as_tensor(fh)).numpy()
+    op = oracle.OraclePlan(k, N, m=4, sigma=2.0, precompute=oracle.FULL)
+    assert oracle.rel_l2(y, op.forward(f)) < 1e-13
+    assert oracle.rel_l2(x, op.adjoint(fh).ravel(order="F")) < 1e-13
+
+
+def test_bench_ndft_checker_matches_oracle():
+    import bench
+    from oracle import oracle
+    rng = np.random.default_rng(3)
+    N, M = (6, 8, 10), 40
+    k = rng.random((3, M)) - 0.5
+    f = rng.standard_normal(N) + 1j * rng.standard_normal(N)
+    fh = rng.standard_normal(M) + 1j * rng.standard_normal(M)
+    sub, lin = np.arange(0, M, 3), np.arange(0, 480, 7)
+    assert oracle.rel_l2(bench.ndft_forward_subset(k, f, sub), oracle.ndft_forward(k, f, subset=sub)) < 1e-13
+    assert oracle.rel_l2(bench.ndft_adjoint_subset(k, N, fh, lin), oracle.ndft_adjoint(k, N, fh, subset=lin)) < 1e-13
