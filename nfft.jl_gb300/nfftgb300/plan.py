@@ -28,6 +28,7 @@ from __future__ import annotations
 import ctypes
 import enum
 import math
+import weakref
 from dataclasses import dataclass, field
 
 import numpy as np
@@ -62,16 +63,44 @@ FULL, TENSOR, LINEAR, POLYNOMIAL = (PrecomputeFlags.FULL, PrecomputeFlags.TENSOR
 WINDOWS = {"kaiser_bessel": 0, "gauss": 1, "spline": 2, "kaiser_bessel_rev": 3, "cosh_type": 4}
 
 
-@dataclass
 class TimingStats:
-    """AbstractNFFTs/src/misc.jl:22-42 (device seconds)."""
-    pre: float = 0.0
-    conv: float = 0.0
-    fft: float = 0.0
-    deconv: float = 0.0
-    conv_adjoint: float = 0.0
-    fft_adjoint: float = 0.0
-    deconv_adjoint: float = 0.0
+    """AbstractNFFTs/src/misc.jl:22-42 (device seconds) of the plan's latest
+    calls.  The plan records CUDA events around its stages; the fields are
+    read from those events when accessed, so timed calls stay asynchronous
+    (reading a field waits for the calls recorded so far)."""
+
+    FIELDS = ("pre", "conv", "fft", "deconv", "conv_adjoint", "fft_adjoint", "deconv_adjoint")
+
+    def __init__(self, pre=0.0, conv=0.0, fft=0.0, deconv=0.0, conv_adjoint=0.0, fft_adjoint=0.0,
+                 deconv_adjoint=0.0):
+        self._vals = [float(pre), float(conv), float(fft), float(deconv), float(conv_adjoint), float(fft_adjoint),
+                      float(deconv_adjoint)]
+        self._source = None  # weak method of the plan returning the 7 values
+
+    def _refresh(self):
+        src = self._source() if self._source is not None else None
+        if src is not None:
+            vals = src()
+            if vals is not None:
+                self._vals = [float(v) for v in vals]
+
+    def __repr__(self):
+        return "TimingStats(" + ", ".join(f"{n}={getattr(self, n):.6g}" for n in self.FIELDS) + ")"
+
+
+def _timing_field(i):
+    def get(self):
+        self._refresh()
+        return self._vals[i]
+
+    def put(self, v):
+        self._vals[i] = float(v)
+
+    return property(get, put)
+
+
+for _i, _n in enumerate(TimingStats.FIELDS):
+    setattr(TimingStats, _n, _timing_field(_i))
 
 
 def reltol_to_params(reltol):
@@ -315,10 +344,7 @@ class GB300NFFTPlan:
             rc = lib.nfft_set_nodes(self._handle, ctypes.c_void_p(kc.ctypes.data), 0)
             self.k = np.asarray(kk, dtype=kc.dtype)
         _check(rc)
-        if self._timing is not None:
-            t = (ctypes.c_double * 7)()
-            _check(lib.nfft_get_timing(self._handle, t))
-            self._timing.pre = t[0]
+        self._timing_update()
         return self
 
     def _destroy_handle(self):
@@ -333,12 +359,17 @@ class GB300NFFTPlan:
                              blockSize=self.params.blockSize, compensated=self.params.compensated,
                              timing=self._timing, device=self.device)
 
+    def _read_timing(self):
+        if self._handle is None or not self._handle.value:
+            return None
+        t = (ctypes.c_double * 7)()
+        _check(L.load().nfft_get_timing(self._handle, t))
+        return tuple(t)
+
     def _timing_update(self):
-        if self._timing is not None:
-            t = (ctypes.c_double * 7)()
-            _check(L.load().nfft_get_timing(self._handle, t))
-            (self._timing.pre, self._timing.conv, self._timing.fft, self._timing.deconv,
-             self._timing.conv_adjoint, self._timing.fft_adjoint, self._timing.deconv_adjoint) = tuple(t)
+        """Bind the plan's TimingStats to this plan's event records (no sync)."""
+        if self._timing is not None and self._timing._source is None:
+            self._timing._source = weakref.WeakMethod(self._read_timing)
 
     def _image(self, f):
         if not isinstance(f, torch.Tensor) or tuple(f.shape) != self.N:

@@ -33,7 +33,7 @@ def _worker(rank, world, port, out):
 def test_max_over_ranks_and_aggregate_gloo():
     world = 2
     port = _free_port()
-    with mp.Manager() as mgr:
+    with mp.get_context("spawn").Manager() as mgr:
         out = mgr.dict()
         mp.spawn(_worker, args=(world, port, out), nprocs=world, join=True)
         res = dict(out)
