@@ -179,8 +179,9 @@ int nfft_grad_nodes(nfft_plan* plan, const void* v, const void* w, void* dk);
 
 /* Tile-shape autotuner (no reference counterpart; the reference's blockSize
  * keyword is chosen by hand, src/precomputation.jl:59-77).  Re-bins the
- * plan's nodes for a set of candidate tile shapes, times one spreading and
- * one gather pass per candidate on the plan's stream, and keeps the fastest.
+ * plan's nodes for a set of candidate tile shapes (and, for D = 3, the two
+ * warp layouts of nfft_set_tiling), times one spreading and one gather pass
+ * per candidate on the plan's stream, and keeps the fastest.
  * With use_cache = 1 the choice is looked up in / stored to the file named by
  * the environment variable NFFT_GB300_TUNE_CACHE, keyed by (D, Ntilde,
  * log2 M, m, precision, SM count, precompute, compensated).  Synchronises. */
@@ -188,6 +189,13 @@ int nfft_autotune(nfft_plan* plan, int use_cache);
 
 /* Re-tile the plan (blockSize) and re-bin its nodes.  Synchronises. */
 int nfft_set_block_size(nfft_plan* plan, const int64_t* block_size);
+
+/* nfft_set_block_size plus the D = 3 spreading warp layout (no reference
+ * counterpart): row_parity_warps = 1 runs 8 warps per tile, each owning the
+ * x-y slices of one residue mod 8; 2 runs 16 warps, each owning one residue
+ * mod 8 and one row parity (for larger tiles).  Ignored for D < 3 and for
+ * compensated plans.  Synchronises. */
+int nfft_set_tiling(nfft_plan* plan, const int64_t* block_size, int row_parity_warps);
 
 /* Plan geometry and sizes. */
 int nfft_get_info(const nfft_plan* plan, nfft_info* info);

@@ -31,13 +31,13 @@ std::string cache_key(const nfft_plan* p) {
   int lm = 0;
   while ((int64_t(1) << (lm + 1)) <= p->M) ++lm;
   char buf[256];
-  snprintf(buf, sizeof(buf), "D%d_N%lldx%lldx%lld_M2^%d_m%d_p%d_sm%d_pre%d_c%d", p->D, (long long)p->Nt[0],
+  snprintf(buf, sizeof(buf), "v2_D%d_N%lldx%lldx%lld_M2^%d_m%d_p%d_sm%d_pre%d_c%d", p->D, (long long)p->Nt[0],
            (long long)p->Nt[1], (long long)p->Nt[2], lm, p->m, p->precision, sms, p->prm.precompute,
            p->prm.compensated);
   return buf;
 }
 
-// Cache file: one line per entry, "key bs0 bs1 bs2".
+// Cache file: one line per entry, "key bs0 bs1 bs2 ny".
 void load_cache() {
   if (g_cache_loaded) return;
   g_cache_loaded = true;
@@ -45,9 +45,13 @@ void load_cache() {
   if (!path) return;
   FILE* f = fopen(path, "r");
   if (!f) return;
-  char key[256];
-  long long a, b, c;
-  while (fscanf(f, "%255s %lld %lld %lld", key, &a, &b, &c) == 4) g_cache[key] = {a, b, c};
+  char line[512];
+  while (fgets(line, sizeof(line), f)) {
+    char key[256];
+    long long a, b, c, ny;
+    if (sscanf(line, "%255s %lld %lld %lld %lld", key, &a, &b, &c, &ny) == 5 && (ny == 1 || ny == 2))
+      g_cache[key] = {a, b, c, ny};
+  }
   fclose(f);
 }
 
@@ -58,23 +62,27 @@ void save_cache() {
   FILE* f = fopen(tmp.c_str(), "w");
   if (!f) return;
   for (auto& kv : g_cache)
-    fprintf(f, "%s %lld %lld %lld\n", kv.first.c_str(), (long long)kv.second[0], (long long)kv.second[1],
-            (long long)kv.second[2]);
+    fprintf(f, "%s %lld %lld %lld %lld\n", kv.first.c_str(), (long long)kv.second[0], (long long)kv.second[1],
+            (long long)kv.second[2], (long long)kv.second[3]);
   fclose(f);
   rename(tmp.c_str(), path);
 }
 
+// Candidate (tile shape, ny): ny = 2 runs 16-warp 3-D tiles owning
+// (slice group, row parity) -- it pays where the tiles are large.
 std::vector<std::vector<int64_t>> candidates(const nfft_plan* p) {
   std::vector<std::vector<int64_t>> c;
   if (p->D == 1) {
-    for (int64_t b : {1024, 2048, 4096, 8192}) c.push_back({b, 1, 1});
+    for (int64_t b : {1024, 2048, 4096, 8192}) c.push_back({b, 1, 1, 1});
   } else if (p->D == 2) {
     for (auto s : std::vector<std::vector<int64_t>>{{32, 32, 1}, {64, 32, 1}, {64, 64, 1}, {128, 64, 1}, {128, 128, 1}})
-      c.push_back(s);
+      c.push_back({s[0], s[1], s[2], 1});
   } else {
     for (auto s : std::vector<std::vector<int64_t>>{{8, 8, 8}, {16, 16, 8}, {16, 16, 16}, {32, 16, 8}, {32, 32, 8},
-                                                     {16, 8, 8}})
-      c.push_back(s);
+                                                     {16, 8, 8}}) {
+      c.push_back({s[0], s[1], s[2], 1});
+      if (!p->prm.compensated && s[1] >= 16) c.push_back({s[0], s[1], s[2], 2});
+    }
   }
   for (auto& s : c)
     for (int d = 0; d < 3; ++d) s[d] = std::min<int64_t>(s[d], p->Nt[d]);
@@ -85,10 +93,9 @@ std::vector<std::vector<int64_t>> candidates(const nfft_plan* p) {
 
 }  // namespace
 
-int spread_pitch_for(int D, int m, int P0, int elem_bytes);
-
-// Apply a tile shape to the plan and re-bin its nodes (from `k`, device).
-int apply_block_size(nfft_plan* p, const int64_t* bs, const void* k) {
+// Apply a tile shape (and 3-D warp layout ny) to the plan and re-bin its
+// nodes (from `k`, device).
+int apply_block_size(nfft_plan* p, const int64_t* bs, const void* k, int ny) {
   int64_t nt = 1;
   int64_t nb[3], tiles[3];
   for (int d = 0; d < 3; ++d) {
@@ -106,10 +113,11 @@ int apply_block_size(nfft_plan* p, const int64_t* bs, const void* k) {
     p->prm.block_size[d] = d < p->D ? nb[d] : 0;
   }
   p->ntiles_total = nt;
+  p->spread_ny = (p->D == 3 && !p->prm.compensated && ny == 2) ? 2 : 1;
   p->spread_pitch = spread_pitch_for(p->D, p->m, int(p->bs[0]) + 2 * p->m - 1,
-                                     int((p->prm.compensated ? 4 : 2) * p->real_size));
+                                     int((p->prm.compensated ? 4 : 2) * p->real_size), p->spread_ny);
   p->gather_pitch = spread_pitch_for(p->D == 2 ? 3 : p->D, p->m, int(p->bs[0]) + 2 * p->m - 1,
-                                     int(2 * p->real_size));
+                                     int(2 * p->real_size), 1);
   return nfft_set_nodes(p, k, 1);
 }
 
@@ -140,7 +148,7 @@ extern "C" int nfft_autotune(nfft_plan* p, int use_cache) {
     std::lock_guard<std::mutex> lock(g_cache_mutex);
     load_cache();
     auto it = g_cache.find(key);
-    if (it != g_cache.end()) return apply_block_size(p, it->second.data(), k);
+    if (it != g_cache.end()) return apply_block_size(p, it->second.data(), k, int(it->second[3]));
   }
   // timing buffers: node values (ones) and the plan's grid
   void* fhat = nullptr;
@@ -154,9 +162,9 @@ extern "C" int nfft_autotune(nfft_plan* p, int use_cache) {
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
   double best = 1e30;
-  std::vector<int64_t> best_bs = {p->bs[0], p->bs[1], p->bs[2]};
+  std::vector<int64_t> best_bs = {p->bs[0], p->bs[1], p->bs[2], p->spread_ny};
   for (const auto& c : candidates(p)) {
-    if (apply_block_size(p, c.data(), k) != NFFT_OK) continue;
+    if (apply_block_size(p, c.data(), k, int(c[3])) != NFFT_OK) continue;
     float times[3];
     bool ok = true;
     for (int r = 0; r < 3 && ok; ++r) {
@@ -176,7 +184,7 @@ extern "C" int nfft_autotune(nfft_plan* p, int use_cache) {
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   cudaGetLastError();  // clear a rejected candidate's error state
-  int rc = apply_block_size(p, best_bs.data(), k);
+  int rc = apply_block_size(p, best_bs.data(), k, int(best_bs[3]));
   if (!rc) {
     std::lock_guard<std::mutex> lock(g_cache_mutex);
     load_cache();
@@ -186,7 +194,13 @@ extern "C" int nfft_autotune(nfft_plan* p, int use_cache) {
   return rc;
 }
 
+extern "C" int nfft_set_tiling(nfft_plan* p, const int64_t* block_size, int row_parity_warps);
+
 extern "C" int nfft_set_block_size(nfft_plan* p, const int64_t* block_size) {
+  return nfft_set_tiling(p, block_size, p ? p->spread_ny : 1);
+}
+
+extern "C" int nfft_set_tiling(nfft_plan* p, const int64_t* block_size, int row_parity_warps) {
   if (!p || !block_size) {
     set_error("null argument");
     return NFFT_ERR_INVALID_ARG;
@@ -196,6 +210,10 @@ extern "C" int nfft_set_block_size(nfft_plan* p, const int64_t* block_size) {
       set_error("block size must be positive");
       return NFFT_ERR_INVALID_ARG;
     }
+  if (row_parity_warps != 1 && row_parity_warps != 2) {
+    set_error("row_parity_warps must be 1 or 2");
+    return NFFT_ERR_INVALID_ARG;
+  }
   if (!p->has_nodes) {
     for (int d = 0; d < 3; ++d) p->prm.block_size[d] = d < p->D ? block_size[d] : 0;
     set_error("plan has no nodes: the block size applies at the next nfft_set_nodes");
@@ -212,7 +230,7 @@ extern "C" int nfft_set_block_size(nfft_plan* p, const int64_t* block_size) {
     set_error("node copy failed");
     rc = NFFT_ERR_CUDA;
   }
-  if (!rc) rc = apply_block_size(p, block_size, k);
+  if (!rc) rc = apply_block_size(p, block_size, k, row_parity_warps);
   cudaFree(k);
   return rc;
 }

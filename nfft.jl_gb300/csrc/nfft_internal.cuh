@@ -130,6 +130,7 @@ struct nfft_plan {
   int64_t n_tasks = 0;
   int4* tasks = nullptr;
   int spread_pitch = 0;            // shared-memory row pitch of the padded spreading tile
+  int spread_ny = 1;               // D = 3: 2 = 16-warp tiles owning (slice group, row parity)
   int gather_pitch = 0;            // shared-memory row pitch of the staged gather tile
   bool gather_tiled = false;       // gather from shared-memory tiles (else straight from L1/L2)
   int* dflag = nullptr;            // device status word
@@ -160,7 +161,9 @@ int launch_build_weight_table(const nfft_plan* p);
 int launch_deconv_factors(nfft_plan* p);
 int launch_build_tasks(nfft_plan* p, int chunk);
 // autotune.cu
-int apply_block_size(nfft_plan* p, const int64_t* bs, const void* k);
+int apply_block_size(nfft_plan* p, const int64_t* bs, const void* k, int ny);
+// spread.cu: bank-conflict-free row pitch of a padded spreading tile
+int spread_pitch_for(int D, int m, int P0, int elem_bytes, int ny);
 // sort.cu
 int radix_sort_pairs(uint32_t* keys, int32_t* vals, uint32_t* keys_tmp, int32_t* vals_tmp, int64_t n,
                      int key_bits, void* scratch, size_t scratch_bytes, cudaStream_t s,

@@ -59,7 +59,6 @@ template <typename T> Nodes<T> make_nodes(const nfft_plan* p) {
   return n;
 }
 
-int spread_pitch_for(int D, int m, int P0, int elem_bytes);
 template Nodes<float> make_nodes<float>(const nfft_plan*);
 template Nodes<double> make_nodes<double>(const nfft_plan*);
 
@@ -450,9 +449,9 @@ int nfft_plan_create(nfft_plan** out, int precision, int D, const int64_t* N, in
   p->lut_size = lut_size_for(p->m);
   default_block(p);
   p->spread_pitch = spread_pitch_for(D, p->m, int(p->bs[0]) + 2 * p->m - 1,
-                                     int((prm.compensated ? 4 : 2) * (precision == 32 ? 4 : 8)));
+                                     int((prm.compensated ? 4 : 2) * (precision == 32 ? 4 : 8)), p->spread_ny);
   p->gather_pitch = spread_pitch_for(D == 2 ? 3 : D, p->m, int(p->bs[0]) + 2 * p->m - 1,
-                                     int(2 * (precision == 32 ? 4 : 8)));
+                                     int(2 * (precision == 32 ? 4 : 8)), 1);
   if (const char* e = getenv("NFFT_GB300_GATHER_TILED")) p->gather_tiled = e[0] == '1';
   p->ntiles_total = 1;
   for (int d = 0; d < 3; ++d) {
@@ -664,6 +663,8 @@ int nfft_plan_copy(const nfft_plan* src, nfft_plan** out) {
   if (!src || !out) return NFFT_ERR_INVALID_ARG;
   int rc = nfft_plan_create(out, src->precision, src->D, src->N, src->M, &src->prm, src->stream);
   if (rc) return rc;
+  (*out)->spread_ny = src->spread_ny;  // same tile shape (prm.block_size), same warp layout
+  (*out)->spread_pitch = src->spread_pitch;
   if (src->has_nodes) {
     rc = nfft_set_nodes(*out, src->k, 1);
     if (rc) {

@@ -75,14 +75,20 @@ int spread_launch(nfft_plan* p, const void* fhat, void* g) {
     }
     auto kern = comp ? (p->wtab ? spread_owned_kernel<D, L, T, true, true> : spread_owned_kernel<D, L, T, false, true>)
                      : (p->wtab ? spread_owned_kernel<D, L, T, true, false> : spread_owned_kernel<D, L, T, false, false>);
+    int threads = OwnedCfg<D, L>::THREADS;
+    if constexpr (D == 3) {
+      if (!comp && p->spread_ny == 2) {  // 16 warps: slice group x row parity
+        kern = p->wtab ? spread_owned_kernel<D, L, T, true, false, 2> : spread_owned_kernel<D, L, T, false, false, 2>;
+        threads = OwnedCfg<D, L, 2>::THREADS;
+      }
+    }
     NFFT_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
     C* fs = static_cast<C*>(p->fsorted);
     int64_t nb = (p->M + 255) / 256;
     if (nb > 152 * 32) nb = 152 * 32;
     sort_values_kernel<T><<<unsigned(nb), 256, 0, p->stream>>>(p->node4, fp, fs, p->M);
     NFFT_LAUNCH_CHECK();
-    kern<<<unsigned(p->n_tasks), OwnedCfg<D, L>::THREADS, smem, p->stream>>>(G, Nd, p->tasks, fs, gp,
-                                                                               p->spread_pitch);
+    kern<<<unsigned(p->n_tasks), threads, smem, p->stream>>>(G, Nd, p->tasks, fs, gp, p->spread_pitch);
   }
   NFFT_LAUNCH_CHECK();
   return NFFT_OK;
@@ -116,12 +122,12 @@ template <typename T> int spread_dispatch(nfft_plan* p, const void* fhat, void* 
 // Row pitch (in accumulator elements) of the padded tile: the smallest pitch
 // >= the padded row length for which every shared-memory access phase of a
 // warp step (lanes = L taps along x times the row slots) hits distinct banks.
-int spread_pitch_for(int D, int m, int P0, int elem_bytes) {
+int spread_pitch_for(int D, int m, int P0, int elem_bytes, int ny) {
   const int L = 2 * m;
-  // lane -> (column ix, row slot ry); D = 3 rows are pitch apart, D = 2 rows
-  // of one warp are 2 slices = 2 pitches apart
+  // lane -> (column ix, row slot ry); D = 3 rows are ny pitches apart (ny = 2:
+  // row-parity ownership), D = 2 rows of one warp are 2 slices = 2 pitches apart
   const int RY = D == 3 ? 32 / L : (D == 2 ? (L + 1) / 2 : 1);
-  const int rowmul = D == 2 ? 2 : 1;
+  const int rowmul = D == 2 ? 2 : (D == 3 ? ny : 1);
   const int words = elem_bytes / 4;       // 32-bit words per element
   const int lanes_per_phase = 32 / words;  // lanes served per shared-memory wavefront
   for (int pitch = P0; pitch < P0 + 64; ++pitch) {

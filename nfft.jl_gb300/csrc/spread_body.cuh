@@ -124,31 +124,36 @@ template <typename A, typename T> __device__ __forceinline__ void kahan_add(A& a
 // --------------------------------------------------------------------------
 // D >= 2: slice-owned, atomic-free.
 //
-// OwnedCfg: NW warps per CTA own the slices along the last dimension with
-// index = warp mod NW.  D = 3: NW = 8, a slice is an x-y plane of L x L taps,
-// lanes = (tap x, row slot), NSTEP steps over the rows.  D = 2: NW = 2, a
+// OwnedCfg: NZ warp groups own the slices along the last dimension with
+// index = group mod NZ.  D = 3: NZ = 8, a slice is an x-y plane of L x L taps,
+// lanes = (tap x, row slot), NSTEP steps over the rows; with NY = 2 the CTA
+// has 16 warps and warp (group, parity) also owns only the padded rows of one
+// parity, so every tile point still has exactly one writer and a warp does
+// half the rows of a node (for L = 8 one 32-tap step).  D = 2: NZ = 2, a
 // warp's taps of one node are ceil(L/2) rows x L columns, flattened over the
 // lanes.  Staging precomputes per node, once per CTA, the complex value times
 // the last-dimension window value of every slice (cz) and the products of the
 // other window values (wxy), so a warp's per-node work is a few shared loads
 // and its read-modify-writes.
-template <int D, int L> struct OwnedCfg {
-  static constexpr int NW = D == 3 ? 8 : 2;
+template <int D, int L, int NY = 1> struct OwnedCfg {
+  static_assert(NY == 1 || (D == 3 && L % 2 == 0), "row-parity ownership needs D = 3");
+  static constexpr int NZ = D == 3 ? 8 : 2;
+  static constexpr int NW = NZ * NY;
   static constexpr int THREADS = NW * 32;
-  static constexpr int KS = (L + NW - 1) / NW;              // owned slices per node (max)
+  static constexpr int KS = (L + NZ - 1) / NZ;              // owned slices per node (max)
   static constexpr int XY = D == 3 ? L * L : L;              // staged products per node
   static constexpr int RY = D == 3 ? 32 / L : 1;             // D = 3 row slots per step
-  static constexpr int NSTEP = D == 3 ? (L + RY - 1) / RY : (KS * L + 31) / 32;
+  static constexpr int NSTEP = D == 3 ? (L / NY + RY - 1) / RY : (KS * L + 31) / 32;
 };
 
-template <int D, int L, typename T, bool TABLE, bool KAHAN>
+template <int D, int L, typename T, bool TABLE, bool KAHAN, int NY = 1>
 __device__ __forceinline__ void spread_owned_body(const Geom<T>& G, const Nodes<T>& Nd, const int4 task,
                                                   const typename Cplx<T>::type* __restrict__ fsorted,
                                                   T* __restrict__ g, int pitch) {
   static_assert(D >= 2, "slice ownership needs D >= 2");
   using C = typename Cplx<T>::type;
   using A = typename Acc<T, KAHAN>::type;
-  using CF = OwnedCfg<D, L>;
+  using CF = OwnedCfg<D, L, NY>;
   constexpr int DL = D * L;
   constexpr int DEG = L + 1;
   constexpr int NB = kStageNodes;
@@ -177,15 +182,17 @@ __device__ __forceinline__ void spread_owned_body(const Geom<T>& G, const Nodes<
     for (int q = threadIdx.x; q < nacc; q += blockDim.x) acc[q] = zero;
   }
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int wz = warp % CF::NZ, wy = warp / CF::NZ;  // slice group, row parity (NY = 2)
   // static per-lane tap pattern: product index and shared offset of each step
+  // (rows NY apart; the node's row parity adds one row for NY = 2)
   int xy_idx[CF::NSTEP], lofs[CF::NSTEP], kslice[CF::NSTEP];
   bool act[CF::NSTEP];
 #pragma unroll
   for (int st = 0; st < CF::NSTEP; ++st) {
     if constexpr (D == 3) {
-      const int ix = lane % L, iy = st * CF::RY + lane / L;
-      act[st] = (lane / L) < CF::RY && iy < L;
-      const int iyc = act[st] ? iy : 0;
+      const int ix = lane % L, rr = st * CF::RY + lane / L;
+      act[st] = (lane / L) < CF::RY && rr < L / NY;
+      const int iyc = act[st] ? NY * rr : 0;
       xy_idx[st] = iyc * L + ix;
       lofs[st] = iyc * pitch + ix;
       kslice[st] = 0;
@@ -228,7 +235,7 @@ __device__ __forceinline__ void spread_owned_body(const Geom<T>& G, const Nodes<
     // stage 1: registers -> shared (window values evaluated here for POLYNOMIAL)
     if (threadIdx.x < n) {
       const int px = r_nd.x - o0, py = r_nd.y - o1;
-      s_meta[threadIdx.x] = D == 3 ? make_int2(r_nd.z - o2, py * pitch + px) : make_int2(py, px);
+      s_meta[threadIdx.x] = D == 3 ? make_int2((r_nd.z - o2) | ((py & 1) << 8), py * pitch + px) : make_int2(py, px);
       s_c[threadIdx.x] = r_c;
     }
 #pragma unroll
@@ -276,37 +283,41 @@ __device__ __forceinline__ void spread_owned_body(const Geom<T>& G, const Nodes<
     // before its stores: one node's taps hit distinct points of the slices.
     const T* xy = s_xy;
     if constexpr (D == 3) {
-      int so_c;
+      int so_c, xo_c;
       C cz_c[CF::KS];
       bool ok_c[CF::KS];
-      auto load_node = [&](int s, int& so, C(&cz)[CF::KS], bool(&ok)[CF::KS]) {
+      // slice offset, row-parity offset of the products, and slice values of node s
+      auto load_node = [&](int s, int& so, int& xo, C(&cz)[CF::KS], bool(&ok)[CF::KS]) {
         const int2 meta = s_meta[s];
-        const int is0 = (warp - meta.x) & (CF::NW - 1);
-        so = (meta.x + is0) * slice_stride + meta.y;
+        const int pz = meta.x & 0xFF;
+        const int is0 = (wz - pz) & (CF::NZ - 1);
+        const int par = NY == 2 ? ((wy - (meta.x >> 8)) & 1) : 0;  // first owned row of the window
+        so = (pz + is0) * slice_stride + meta.y + par * pitch;
+        xo = par * L;
 #pragma unroll
         for (int k = 0; k < CF::KS; ++k) {
-          const int is = is0 + k * CF::NW;
+          const int is = is0 + k * CF::NZ;
           ok[k] = is < L;
           cz[k] = s_cz[s * L + (ok[k] ? is : 0)];
         }
       };
-      load_node(0, so_c, cz_c, ok_c);
+      load_node(0, so_c, xo_c, cz_c, ok_c);
       for (int s = 0; s < n; ++s, xy += CF::XY) {
-        int so_n;
+        int so_n, xo_n;
         C cz_n[CF::KS];
         bool ok_n[CF::KS];
-        load_node(s + 1 < n ? s + 1 : s, so_n, cz_n, ok_n);
+        load_node(s + 1 < n ? s + 1 : s, so_n, xo_n, cz_n, ok_n);
 #pragma unroll
         for (int k = 0; k < CF::KS; ++k) {
           if (ok_c[k]) {
-            const int so = so_c + k * CF::NW * slice_stride;
+            const int so = so_c + k * CF::NZ * slice_stride;
             A a[CF::NSTEP];
             T w[CF::NSTEP];
 #pragma unroll
             for (int st = 0; st < CF::NSTEP; ++st) {
               if (act[st]) {
                 a[st] = acc[so + lofs[st]];
-                w[st] = xy[xy_idx[st]];
+                w[st] = xy[xo_c + xy_idx[st]];
               }
             }
 #pragma unroll
@@ -320,6 +331,7 @@ __device__ __forceinline__ void spread_owned_body(const Geom<T>& G, const Nodes<
           }
         }
         so_c = so_n;
+        xo_c = xo_n;
 #pragma unroll
         for (int k = 0; k < CF::KS; ++k) {
           cz_c[k] = cz_n[k];
@@ -330,7 +342,7 @@ __device__ __forceinline__ void spread_owned_body(const Geom<T>& G, const Nodes<
       int2 meta_c = s_meta[0];
       for (int s = 0; s < n; ++s, xy += CF::XY) {
         const int2 meta_n = s_meta[s + 1 < n ? s + 1 : s];
-        const int is0 = (warp - meta_c.x) & (CF::NW - 1);
+        const int is0 = (wz - meta_c.x) & (CF::NZ - 1);
         A a[CF::NSTEP];
         T w[CF::NSTEP];
         C cz[CF::NSTEP];
@@ -338,7 +350,7 @@ __device__ __forceinline__ void spread_owned_body(const Geom<T>& G, const Nodes<
         bool ok[CF::NSTEP];
 #pragma unroll
         for (int st = 0; st < CF::NSTEP; ++st) {
-          const int is = is0 + kslice[st] * CF::NW;
+          const int is = is0 + kslice[st] * CF::NZ;
           ok[st] = act[st] && is < L;
           if (ok[st]) {
             off[st] = (meta_c.x + is) * slice_stride + meta_c.y + lofs[st];
@@ -365,12 +377,12 @@ __device__ __forceinline__ void spread_owned_body(const Geom<T>& G, const Nodes<
   flush_tile<D, T, KAHAN, CF::NW>(G, acc, g, o0, o1, o2, P0, P1, P2, pitch);
 }
 
-template <int D, int L, typename T, bool TABLE, bool KAHAN>
-__global__ void __launch_bounds__(OwnedCfg<D, L>::THREADS) spread_owned_kernel(Geom<T> G, Nodes<T> Nd,
+template <int D, int L, typename T, bool TABLE, bool KAHAN, int NY = 1>
+__global__ void __launch_bounds__(OwnedCfg<D, L, NY>::THREADS) spread_owned_kernel(Geom<T> G, Nodes<T> Nd,
                                                                                const int4* __restrict__ tasks,
                                                                                const typename Cplx<T>::type* __restrict__ fsorted,
                                                                                T* __restrict__ g, int pitch) {
-  spread_owned_body<D, L, T, TABLE, KAHAN>(G, Nd, tasks[blockIdx.x], fsorted, g, pitch);
+  spread_owned_body<D, L, T, TABLE, KAHAN, NY>(G, Nd, tasks[blockIdx.x], fsorted, g, pitch);
 }
 
 // --------------------------------------------------------------------------

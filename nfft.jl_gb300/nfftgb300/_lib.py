@@ -90,6 +90,7 @@ SIGNATURES = {
     "nfft_get_deconv_factors": (_I, [_P, _P]),
     "nfft_sync": (_I, [_P]),
     "nfft_bin_nodes_noalloc": (_I, [_I, _I, _I64P, _I64P, _I64, _P, _P, _P, _P]),
+    "nfft_set_tiling": (_I, [_P, _I64P, _I]),
     "nfft_batch_create": (_I, [_P, _P, _I, _P]),
     "nfft_batch_destroy": (_I, [_P]),
     "nfft_batch_forward": (_I, [_P, _P, _P]),

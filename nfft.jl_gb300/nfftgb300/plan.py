@@ -493,11 +493,15 @@ class GB300NFFTPlan:
         self._refresh_info()
         return self.params.blockSize
 
-    def set_block_size(self, bs):
-        """Re-tile the plan (blockSize) and re-bin its nodes."""
+    def set_block_size(self, bs, row_parity_warps=None):
+        """Re-tile the plan (blockSize) and re-bin its nodes; for D = 3,
+        row_parity_warps = 2 spreads with 16 warps per tile (nfft_set_tiling)."""
         arr = (ctypes.c_int64 * 3)(*(list(bs) + [1] * (3 - len(bs))))
         self._sync_stream()
-        _check(L.load().nfft_set_block_size(self._handle, arr))
+        if row_parity_warps is None:
+            _check(L.load().nfft_set_block_size(self._handle, arr))
+        else:
+            _check(L.load().nfft_set_tiling(self._handle, arr, int(row_parity_warps)))
         self._refresh_info()
         return self.params.blockSize
 

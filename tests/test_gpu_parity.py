@@ -241,3 +241,33 @@ def test_compensated_spreading_keeps_small_addends(D, N):
         errs[comp] = oracle.rel_l2(colmajor_flat(g.cpu().numpy()), colmajor_flat(ref))
     assert errs[False] > 1e-5, errs
     assert errs[True] < 1e-6, errs
+
+
+@pytest.mark.parametrize("dtype,m", [(np.float64, m) for m in (2, 3, 4, 5, 6, 7, 8)] +
+                         [(np.float32, m) for m in (2, 3, 4, 5, 6)])
+def test_row_parity_spreading_layout(dtype, m):
+    """16-warp 3-D spreading tiles (nfft_set_tiling with row-parity
+    ownership) give the oracle's adjoint for every window width, tile shape
+    and precision, like the 8-warp layout.  Tiles whose padded accumulator
+    exceeds shared memory are refused (NotImplementedError) and skipped.
+    FP32 stops at m = 6: the unnormalised Kaiser-Bessel window reaches
+    ~5e12 per dimension at m = 7, so 3-D products overflow FP32 -- as in the
+    reference's Float32 plan."""
+    N = (24, 20, 16)
+    k, f, fhat = rand_problem(3, N, 6000, seed=90 + m, dtype=dtype)
+    p = nf.plan_nfft(k, N, m=m, sigma=2.0, precompute=oracle.TENSOR, blockSize=(4, 4, 4))
+    op = oracle.OraclePlan(k.astype(np.float64), N, m=m, sigma=2.0)
+    ref = colmajor_flat(op.adjoint(fhat))
+    tol = TOL64 if dtype == np.float64 else TOL32
+    v = torch.as_tensor(fhat).to(p.cdtype)
+    ran = 0
+    for bs in [(4, 4, 4), (16, 16, 8), (8, 8, 8), (16, 16, 16), (32, 16, 8)]:
+        for rp in (1, 2):
+            p.set_block_size(bs, row_parity_warps=rp)
+            try:
+                x = (nf.adjoint(p) * v).cpu().numpy()
+            except NotImplementedError:
+                continue
+            ran += 1
+            assert oracle.rel_l2(colmajor_flat(x), ref) < tol, (bs, rp)
+    assert ran >= 2
