@@ -642,8 +642,15 @@ int nfft_set_nodes(nfft_plan* p, const void* k, int k_on_device) {
                      sizeof(int4) * size_t(M) + rs * 4 * size_t(M) + (table ? rs * size_t(M * D * L) : 0) +
                      sizeof(int32_t) * size_t(nt + 1);
   if (p->prm.blocking) {
-    // hot tiles are split into chunks of at most 1024 nodes
-    rc = launch_build_tasks(p, 1024);
+    // hot tiles are split into chunks of at most `chunk` nodes (each chunk is
+    // one spreading task and flushes its padded tile once);
+    // NFFT_GB300_TASK_CHUNK overrides the default 1024
+    int chunk = 1024;
+    if (const char* e = getenv("NFFT_GB300_TASK_CHUNK")) {
+      const int c = atoi(e);
+      if (c >= 32 && c <= (1 << 20)) chunk = c;
+    }
+    rc = launch_build_tasks(p, chunk);
     if (rc) return rc;
     if (cudaMalloc(&p->fsorted, 2 * rs * size_t(M > 0 ? M : 1)) != cudaSuccess) {
       set_error("cudaMalloc of the sorted value buffer failed");

@@ -255,24 +255,24 @@ __device__ __forceinline__ void spread_owned_body(const Geom<T>& G, const Nodes<
       }
     }
     __syncthreads();
-    // stage 2: per-slice values and tap products
-    for (int q = threadIdx.x; q < n * (L + CF::XY); q += blockDim.x) {
-      const int s = q / (L + CF::XY), r = q - s * (L + CF::XY);
-      if (r < L) {
-        const T wl = s_w[s * DL + (D - 1) * L + r];
-        const C c = s_c[s];
-        C v;
-        v.x = c.x * wl;
-        v.y = c.y * wl;
-        s_cz[s * L + r] = v;
+    // stage 2: per-slice values, then tap products (two uniform loops over
+    // contiguous items: no divergence between the two kinds of item)
+    for (int q = threadIdx.x; q < n * L; q += blockDim.x) {
+      const int s = q / L, r = q - s * L;
+      const T wl = s_w[s * DL + (D - 1) * L + r];
+      const C c = s_c[s];
+      C v;
+      v.x = c.x * wl;
+      v.y = c.y * wl;
+      s_cz[q] = v;
+    }
+    for (int q = threadIdx.x; q < n * CF::XY; q += blockDim.x) {
+      const int s = q / CF::XY, u = q - s * CF::XY;
+      if constexpr (D == 3) {
+        const int iy = u / L, jx = u - iy * L;
+        s_xy[q] = s_w[s * DL + jx] * s_w[s * DL + L + iy];
       } else {
-        const int u = r - L;
-        if constexpr (D == 3) {
-          const int iy = u / L, jx = u - iy * L;
-          s_xy[s * CF::XY + u] = s_w[s * DL + jx] * s_w[s * DL + L + iy];
-        } else {
-          s_xy[s * CF::XY + u] = s_w[s * DL + u];
-        }
+        s_xy[q] = s_w[s * DL + u];
       }
     }
     __syncthreads();
