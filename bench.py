@@ -46,7 +46,7 @@ WORKLOAD = "3D radial koosh-ball NFFT fwd+adj, N=256^3, 8192 spokes x 512 sample
 # (profiles/spread_owned_radial256.md: 1.115 GB read + 0.564 GB write).
 SPREAD_DRAM_BYTES = 1.679e9
 # What bounds the dominant kernel on chip (same capture).
-SPREAD_LIMITER = ("shared-memory pipe 70.7% and instruction issue 80.8% of peak (ncu); the 20 B of shared-memory "
+SPREAD_LIMITER = ("shared-memory pipe 73.3% and instruction issue 81.6% of peak (ncu); the 20 B of shared-memory "
                   "traffic per tap put the tap phase at 1.07 ms, HBM is not the limiter")
 
 
