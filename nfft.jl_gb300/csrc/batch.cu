@@ -4,11 +4,13 @@
 // Every stage runs as ONE launch over all plans (a per-plan descriptor table
 // in device memory, plans found by binary search over prefix sums):
 //   forward:  pad+apodize (grid-stride over all plans' grid pairs), the
-//             plans' cuFFT transforms, gather (persistent warps over all
-//             plans' nodes);
+//             plans' FFTs, gather (persistent warps over all plans' nodes);
 //   adjoint:  grid zero-fill, value sort, spreading (persistent CTAs taking
-//             tasks of all plans from one atomic counter), the plans' cuFFT
-//             transforms, crop+apodize.
+//             tasks of all plans from one atomic counter), the plans' FFTs,
+//             crop+apodize.
+// The plans' FFTs run concurrently on forked streams: the fused pruned FFT
+// (with its own pad / crop, reading the image pointer from the per-call
+// table) for power-of-two grids, cuFFT for the others.
 // The whole sequence of a direction is captured once into a CUDA graph and
 // replayed; per call only the table of input/output pointers is copied.
 // Plans in a batch share precision, dimension (2 or 3), m, window-evaluation
@@ -230,7 +232,20 @@ int forked_ffts(nfft_batch* B, int dir) {
   for (int i = 0; i < B->n && !rc; ++i) {
     nfft_plan* p = B->plans[i];
     rc = nfft_set_stream(p, B->side[i % ns]);
-    if (!rc) rc = exec_fft_plan(p, dir);
+    if (rc) break;
+    if (p->fused_fft) {
+      // fused pruned FFT with pad (forward) or crop (adjoint) inside; the
+      // image pointer is read from the batch's per-call pointer table
+      if (dir == CUFFT_FORWARD) {
+        rc = fused_forward_x(p, nullptr, B->d_ptrs + 2 * i);
+        if (!rc) rc = fused_forward_lines(p);
+      } else {
+        rc = fused_adjoint_lines(p);
+        if (!rc) rc = fused_adjoint_x(p, nullptr, B->d_ptrs + 2 * i + 1);
+      }
+    } else {
+      rc = exec_fft_plan(p, dir);
+    }
   }
   for (int s = 0; s < ns; ++s) {
     NFFT_CUDA_TRY(cudaEventRecord(B->join_ev[s], B->side[s]));
@@ -335,7 +350,9 @@ template <typename T> int fill_items(nfft_batch* B) {
     it.inv[1] = p->D > 1 ? inv + p->N[0] : inv + nsum;
     it.inv[2] = p->D > 2 ? inv + p->N[0] + p->N[1] : inv + nsum;
     const int64_t grid = p->Nt[0] * p->Nt[1] * p->Nt[2];
-    const int64_t sizes[5] = {grid / 2, p->M, p->n_tasks, p->N[0] * p->N[1] * p->N[2], grid};
+    // plans on the fused pruned FFT pad and crop inside their x-line kernels
+    const int64_t sizes[5] = {p->fused_fft ? 0 : grid / 2, p->M, p->n_tasks,
+                              p->fused_fft ? 0 : p->N[0] * p->N[1] * p->N[2], grid};
     for (int a = 0; a < 5; ++a) base[a * (B->n + 1) + i + 1] = base[a * (B->n + 1) + i] + sizes[a];
   }
   for (int a = 0; a < 5; ++a) B->total[a] = base[a * (B->n + 1) + B->n];

@@ -221,8 +221,9 @@ template <typename T> struct Inv3 {
 // forward X: image rows -> deconvolved, zero-padded, transformed grid rows
 template <typename T, int NX, int W>
 __global__ void __launch_bounds__(kFftThreads, fft_min_blocks<T, NX, true>()) fft_x_pad_kernel(FftGeom G, Inv3<T> inv, const Cx<T>* __restrict__ f,
-                                                                Cx<T>* __restrict__ g, const Cx<T>* __restrict__ tw) {
+                                                                Cx<T>* __restrict__ g, const Cx<T>* __restrict__ tw, void* const* slot) {
   using C = Cx<T>;
+  if (slot) f = static_cast<const C*>(slot[0]);  // image pointer read from device memory
   extern __shared__ __align__(16) unsigned char fft_smem[];
   C* buf = reinterpret_cast<C*>(fft_smem);
   constexpr int P = W + 1;
@@ -289,7 +290,8 @@ __global__ void __launch_bounds__(kFftThreads, fft_min_blocks<T, NX, true>()) ff
 // adjoint X': grid rows of the image -> transformed, cropped, deconvolved image rows
 template <typename T, int NX, int W>
 __global__ void __launch_bounds__(kFftThreads, fft_min_blocks<T, NX, false>()) fft_x_crop_kernel(FftGeom G, Inv3<T> inv, const Cx<T>* __restrict__ g,
-                                                                 Cx<T>* __restrict__ f, const Cx<T>* __restrict__ tw) {
+                                                                 Cx<T>* __restrict__ f, const Cx<T>* __restrict__ tw, void* const* slot) {
+  if (slot) f = static_cast<Cx<T>*>(slot[0]);  // image pointer read from device memory
   using C = Cx<T>;
   extern __shared__ __align__(16) unsigned char fft_smem[];
   C* buf = reinterpret_cast<C*>(fft_smem);
@@ -546,9 +548,14 @@ template <int NX, bool FWD>
 __global__ void __launch_bounds__(256, FWD ? 3 : 2) fft4_x_kernel(FftGeom G, Inv3<float> inv,
                                                                   const float2* __restrict__ src,
                                                                   float2* __restrict__ dst,
-                                                                  const float2* __restrict__ tw) {
+                                                                  const float2* __restrict__ tw,
+                                                                  void* const* slot) {
   using C = float2;
   constexpr int R1 = Split4<NX>::R1, R2 = Split4<NX>::R2, W = kW4, PR = R1 + 1, PW = R2 * PR, S = FWD ? -1 : 1;
+  if (slot) {  // the image pointer is read from device memory (graph replays with new arrays)
+    if (FWD) src = static_cast<const float2*>(slot[0]);
+    else dst = static_cast<float2*>(slot[0]);
+  }
   extern __shared__ __align__(16) unsigned char fft_smem[];
   C* y = reinterpret_cast<C*>(fft_smem);
   __shared__ float s_row[W];
@@ -661,7 +668,7 @@ template <typename K> int set_smem(K kern, size_t bytes) {
   return NFFT_OK;
 }
 
-template <typename T, int NX> int x_pass_t(nfft_plan* p, const void* src, void* dst, bool fwd) {
+template <typename T, int NX> int x_pass_t(nfft_plan* p, const void* src, void* dst, bool fwd, void* const* slot) {
   using C = Cx<T>;
   if constexpr (sizeof(T) == 4 && NX <= 512 && NFFT_FFT_FOURSTEP) {
     const size_t smem = size_t(kW4) * Split4<NX>::R2 * (Split4<NX>::R1 + 1) * sizeof(float2);
@@ -670,7 +677,7 @@ template <typename T, int NX> int x_pass_t(nfft_plan* p, const void* src, void* 
     auto kern = fwd ? fft4_x_kernel<NX, true> : fft4_x_kernel<NX, false>;
     if (int rc = set_smem(kern, smem)) return rc;
     kern<<<blocks, 256, smem, p->stream>>>(make_fft_geom(p), make_inv3<float>(p), static_cast<const float2*>(src),
-                                           static_cast<float2*>(dst), tw);
+                                           static_cast<float2*>(dst), tw, slot);
     NFFT_LAUNCH_CHECK();
     return NFFT_OK;
   }
@@ -683,12 +690,12 @@ template <typename T, int NX> int x_pass_t(nfft_plan* p, const void* src, void* 
     auto kern = fft_x_pad_kernel<T, NX, W>;
     if (int rc = set_smem(kern, smem)) return rc;
     kern<<<blocks, kFftThreads, smem, p->stream>>>(make_fft_geom(p), make_inv3<T>(p), static_cast<const C*>(src),
-                                                   static_cast<C*>(dst), tw);
+                                                   static_cast<C*>(dst), tw, slot);
   } else {
     auto kern = fft_x_crop_kernel<T, NX, W>;
     if (int rc = set_smem(kern, smem)) return rc;
     kern<<<blocks, kFftThreads, smem, p->stream>>>(make_fft_geom(p), make_inv3<T>(p), static_cast<const C*>(src),
-                                                   static_cast<C*>(dst), tw);
+                                                   static_cast<C*>(dst), tw, slot);
   }
   NFFT_LAUNCH_CHECK();
   return NFFT_OK;
@@ -741,13 +748,13 @@ template <typename T, int NL> int line_pass_t(nfft_plan* p, int axis, bool fwd) 
   return NFFT_OK;
 }
 
-template <typename T> int x_pass(nfft_plan* p, const void* src, void* dst, bool fwd) {
+template <typename T> int x_pass(nfft_plan* p, const void* src, void* dst, bool fwd, void* const* slot) {
   switch (p->Nt[0]) {
-    case 64: return x_pass_t<T, 64>(p, src, dst, fwd);
-    case 128: return x_pass_t<T, 128>(p, src, dst, fwd);
-    case 256: return x_pass_t<T, 256>(p, src, dst, fwd);
-    case 512: return x_pass_t<T, 512>(p, src, dst, fwd);
-    case 1024: return x_pass_t<T, 1024>(p, src, dst, fwd);
+    case 64: return x_pass_t<T, 64>(p, src, dst, fwd, slot);
+    case 128: return x_pass_t<T, 128>(p, src, dst, fwd, slot);
+    case 256: return x_pass_t<T, 256>(p, src, dst, fwd, slot);
+    case 512: return x_pass_t<T, 512>(p, src, dst, fwd, slot);
+    case 1024: return x_pass_t<T, 1024>(p, src, dst, fwd, slot);
   }
   set_error("fused FFT: unsupported length %lld", (long long)p->Nt[0]);
   return NFFT_ERR_UNSUPPORTED;
@@ -805,8 +812,11 @@ int fused_fft_init(nfft_plan* p) {
 
 // forward: image f -> transformed grid (pad + deconvolve + FFT).  The X
 // kernel is stage 1, the Y / Z line passes stage 2 (for the timing ring).
-int fused_forward_x(nfft_plan* p, const void* f) {
-  return p->precision == 32 ? x_pass<float>(p, f, p->grid, true) : x_pass<double>(p, f, p->grid, true);
+// With f_slot (device memory holding the image pointer) the kernels read the
+// pointer at run time, so a captured graph replays with new arrays.
+int fused_forward_x(nfft_plan* p, const void* f, void* const* f_slot) {
+  return p->precision == 32 ? x_pass<float>(p, f, p->grid, true, f_slot)
+                            : x_pass<double>(p, f, p->grid, true, f_slot);
 }
 int fused_forward_lines(nfft_plan* p) {
   int rc;
@@ -831,8 +841,9 @@ int fused_adjoint_lines(nfft_plan* p) {
   }
   return rc;
 }
-int fused_adjoint_x(nfft_plan* p, void* f) {
-  return p->precision == 32 ? x_pass<float>(p, p->grid, f, false) : x_pass<double>(p, p->grid, f, false);
+int fused_adjoint_x(nfft_plan* p, void* f, void* const* f_slot) {
+  return p->precision == 32 ? x_pass<float>(p, p->grid, f, false, f_slot)
+                            : x_pass<double>(p, p->grid, f, false, f_slot);
 }
 
 }  // namespace nfft

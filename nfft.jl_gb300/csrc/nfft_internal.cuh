@@ -185,10 +185,10 @@ int launch_spread(nfft_plan* p, const void* fhat, int fhat_real, void* g, int g_
 int exec_fft_plan(nfft_plan* p, int dir);
 // fft.cu: fused pruned FFT with the deconvolution
 int fused_fft_init(nfft_plan* p);
-int fused_forward_x(nfft_plan* p, const void* f);
+int fused_forward_x(nfft_plan* p, const void* f, void* const* f_slot = nullptr);
 int fused_forward_lines(nfft_plan* p);
 int fused_adjoint_lines(nfft_plan* p);
-int fused_adjoint_x(nfft_plan* p, void* f);
+int fused_adjoint_x(nfft_plan* p, void* f, void* const* f_slot = nullptr);
 // gradk.cu
 int launch_grad_nodes(const nfft_plan* p, const void* g, const void* w, void* dk);
 // plain.cu (per-node kernels of the plain path, blocking = 0)
