@@ -104,7 +104,10 @@ function AbstractNFFTs.plan_nfft(::GB300Backend, ::Type{<:CuArray}, k::Matrix{T}
                                  window::Symbol=:kaiser_bessel, precompute=AbstractNFFTs.POLYNOMIAL,
                                  blocking::Bool=true, sortNodes::Bool=false, storeDeconvolutionIdx::Bool=false,
                                  blockSize=nothing, kwargs...) where {T<:Union{Float32,Float64},D}
-  dims != 1:D && error("GPU NFFT does not work along directions right now!")
+  dims_ = dims isa Integer ? (dims:dims) : dims
+  if dims_ != 1:D
+    return GB300DirectionalPlan(k, N, dims_; window, kwargs...)
+  end
   size(k, 1) == D || throw(ArgumentError("Nodes x have dimension $(size(k,1)) != $D"))
   haskey(WINDOWS, window) || error("Window $(window) not yet implemented!")
   t = @elapsed begin
@@ -240,6 +243,141 @@ end
 function Base.copy(p::GB300NFFTPlan{T,D}) where {T,D}
   AbstractNFFTs.plan_nfft(GB300Backend(), CuArray, copy(p.k), p.N; m=p.params.m, σ=p.params.σ,
                           window=p.params.window, precompute=p.params.precompute, blocking=p.params.blocking)
+end
+
+"""
+    autotune!(p; use_cache=true)
+
+Pick the spreading tile shape (and 3-D warp layout) by timing the plan's own
+nodes (`nfft_autotune`); the choice is cached in the file named by
+`NFFT_GB300_TUNE_CACHE`.
+"""
+function autotune!(p::GB300NFFTPlan; use_cache::Bool=true)
+  bind_stream!(p)
+  check(ccall((:nfft_autotune, libnfft[]), Cint, (Ptr{Cvoid}, Cint), p.handle, use_cache))
+  return p
+end
+
+"""
+    set_tiling!(p, blockSize; row_parity_warps=1)
+
+Re-tile the plan (the reference's `blockSize`) and re-bin its nodes; for
+D = 3, `row_parity_warps = 2` spreads with 16 warps per tile.
+"""
+function set_tiling!(p::GB300NFFTPlan, blockSize; row_parity_warps::Integer=1)
+  bs = Int64[ntuple(d -> d <= length(blockSize) ? blockSize[d] : 1, 3)...]
+  bind_stream!(p)
+  check(ccall((:nfft_set_tiling, libnfft[]), Cint, (Ptr{Cvoid}, Ptr{Int64}, Cint), p.handle, bs, row_parity_warps))
+  return p
+end
+
+# ------------------------------------------------------------ directional plans
+
+"""
+    GB300DirectionalPlan
+
+`plan_nfft(CuArray, k, N; dims)` with `dims` a contiguous range that is not
+1:D (src/implementation.jl:73-104, src/directional.jl): the NFFT along `dims`,
+every other index a batch column; `NOut` replaces the `dims` range of `N` by
+J.  LINEAR window, as in the reference.
+"""
+mutable struct GB300DirectionalPlan{T,D,R} <: AbstractNFFTPlan{T,D,R}
+  handle::Ptr{Cvoid}
+  N::NTuple{D,Int}
+  NOut::NTuple{R,Int}
+  J::Int
+  k::Matrix{T}
+  dims::UnitRange{Int}
+end
+
+function GB300DirectionalPlan(k::Matrix{T}, N::NTuple{D,Int}, dims::UnitRange{Int}; window::Symbol=:kaiser_bessel,
+                              kwargs...) where {T<:Union{Float32,Float64},D}
+  size(k, 1) == length(dims) || throw(ArgumentError("Nodes x have dimension $(size(k,1)) != $(length(dims))"))
+  (first(dims) >= 1 && last(dims) <= D) || throw(ArgumentError("dims $dims do not fit $D dimensions"))
+  m, σ, reltol = AbstractNFFTs.accuracyParams(; kwargs...)
+  cp = CParams(m, σ, WINDOWS[window], Int(AbstractNFFTs.LINEAR), false, false, false, (0, 0, 0), 0, 0)
+  Nc = Int64[N...; ones(Int64, 3 - D)]
+  h = Ref{Ptr{Cvoid}}(C_NULL)
+  check(ccall((:nfft_dplan_create, libnfft[]), Cint,
+              (Ref{Ptr{Cvoid}}, Cint, Cint, Ptr{Int64}, Cint, Cint, Int64, Ref{CParams}, Ptr{Cvoid}),
+              h, T == Float32 ? 32 : 64, D, Nc, first(dims) - 1, last(dims) - 1, size(k, 2), cp, CUDA.stream().handle))
+  J = size(k, 2)
+  NOut = (N[1:first(dims)-1]..., J, N[last(dims)+1:end]...)
+  p = GB300DirectionalPlan{T,D,length(NOut)}(h[], N, NOut, J, k, dims)
+  finalizer(p) do q
+    q.handle == C_NULL || ccall((:nfft_dplan_destroy, libnfft[]), Cint, (Ptr{Cvoid},), q.handle)
+    q.handle = C_NULL
+  end
+  check(ccall((:nfft_dplan_set_nodes, libnfft[]), Cint, (Ptr{Cvoid}, Ptr{T}, Cint), p.handle, k, 0))
+  return p
+end
+
+AbstractNFFTs.size_in(p::GB300DirectionalPlan) = p.N
+AbstractNFFTs.size_out(p::GB300DirectionalPlan) = p.NOut
+
+function LinearAlgebra.mul!(fHat::CuArray{Complex{T}}, p::GB300DirectionalPlan{T,D},
+                            f::CuArray{Complex{T},D}) where {T,D}
+  (size(f) == p.N && size(fHat) == p.NOut) || throw(DimensionMismatch("Data is not consistent with NFFTPlan"))
+  check(ccall((:nfft_dplan_set_stream, libnfft[]), Cint, (Ptr{Cvoid}, Ptr{Cvoid}), p.handle, CUDA.stream().handle))
+  check(ccall((:nfft_dplan_forward, libnfft[]), Cint, (Ptr{Cvoid}, CuPtr{Complex{T}}, CuPtr{Complex{T}}),
+              p.handle, f, fHat))
+  return fHat
+end
+
+function LinearAlgebra.mul!(f::CuArray{Complex{T},D}, pl::Adjoint{Complex{T},<:GB300DirectionalPlan{T,D}},
+                            fHat::CuArray{Complex{T}}) where {T,D}
+  p = pl.parent
+  (size(f) == p.N && size(fHat) == p.NOut) || throw(DimensionMismatch("Data is not consistent with NFFTPlan"))
+  check(ccall((:nfft_dplan_set_stream, libnfft[]), Cint, (Ptr{Cvoid}, Ptr{Cvoid}), p.handle, CUDA.stream().handle))
+  check(ccall((:nfft_dplan_adjoint, libnfft[]), Cint, (Ptr{Cvoid}, CuPtr{Complex{T}}, CuPtr{Complex{T}}),
+              p.handle, fHat, f))
+  return f
+end
+
+# ---------------------------------------------------------------- batched plans
+
+"""
+    GB300Batch(plans)
+
+Many plans of uneven N and M transformed together (`nfft_batch_*`, no
+reference counterpart): one launch per stage over all plans, replayed from a
+CUDA graph captured on the current stream.  `batch_mul!(fHats, b, fs)` and
+`batch_mul_adjoint!(fs, b, fHats)` transform every plan.
+"""
+mutable struct GB300Batch
+  handle::Ptr{Cvoid}
+  plans::Vector{GB300NFFTPlan}
+end
+
+function GB300Batch(plans::Vector{<:GB300NFFTPlan})
+  h = Ref{Ptr{Cvoid}}(C_NULL)
+  handles = Ptr{Cvoid}[p.handle for p in plans]
+  check(ccall((:nfft_batch_create, libnfft[]), Cint, (Ref{Ptr{Cvoid}}, Ptr{Ptr{Cvoid}}, Cint, Ptr{Cvoid}),
+              h, handles, length(plans), CUDA.stream().handle))
+  b = GB300Batch(h[], Vector{GB300NFFTPlan}(plans))
+  finalizer(b) do q
+    q.handle == C_NULL || ccall((:nfft_batch_destroy, libnfft[]), Cint, (Ptr{Cvoid},), q.handle)
+    q.handle = C_NULL
+  end
+  return b
+end
+
+function batch_mul!(fHats::Vector{<:CuVector}, b::GB300Batch, fs::Vector{<:CuArray})
+  length(fHats) == length(fs) == length(b.plans) || throw(DimensionMismatch("one input and output per plan"))
+  fp = Ptr{Cvoid}[Ptr{Cvoid}(UInt(pointer(f))) for f in fs]
+  hp = Ptr{Cvoid}[Ptr{Cvoid}(UInt(pointer(v))) for v in fHats]
+  check(ccall((:nfft_batch_forward, libnfft[]), Cint, (Ptr{Cvoid}, Ptr{Ptr{Cvoid}}, Ptr{Ptr{Cvoid}}),
+              b.handle, fp, hp))
+  return fHats
+end
+
+function batch_mul_adjoint!(fs::Vector{<:CuArray}, b::GB300Batch, fHats::Vector{<:CuVector})
+  length(fHats) == length(fs) == length(b.plans) || throw(DimensionMismatch("one input and output per plan"))
+  fp = Ptr{Cvoid}[Ptr{Cvoid}(UInt(pointer(f))) for f in fs]
+  hp = Ptr{Cvoid}[Ptr{Cvoid}(UInt(pointer(v))) for v in fHats]
+  check(ccall((:nfft_batch_adjoint, libnfft[]), Cint, (Ptr{Cvoid}, Ptr{Ptr{Cvoid}}, Ptr{Ptr{Cvoid}}),
+              b.handle, hp, fp))
+  return fs
 end
 
 Base.show(io::IO, p::GB300NFFTPlan) =

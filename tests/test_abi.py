@@ -66,3 +66,16 @@ def test_plan_create_rejects_bad_arguments_without_gpu(lib):
     prm.precompute = 0
     assert lib.nfft_plan_create(ctypes.byref(h), 32, 2, N, 10, ctypes.byref(prm), None) == L.NFFT_ERR_UNSUPPORTED
     assert not h.value
+
+
+def test_julia_backend_binds_the_interface_entry_points():
+    """The Julia ccall backend (not executable here: no Julia) binds every
+    entry point the AbstractNFFTs interface, directional plans and batches
+    need; the remaining header functions are inspection / tuning helpers."""
+    jl = open(os.path.join(ROOT, "nfft.jl_gb300", "julia", "NFFTGB300.jl")).read()
+    helpers = {"nfft_bin_nodes_noalloc", "nfft_get_binning", "nfft_get_deconv_factors", "nfft_get_timing_totals",
+               "nfft_kernel_launch_count", "nfft_params_default", "nfft_plan_copy", "nfft_set_block_size",
+               "nfft_sync", "nfft_timing_reset"}
+    for n in declared_functions():
+        if n not in helpers:
+            assert f":{n}" in jl, n
