@@ -271,3 +271,20 @@ def test_row_parity_spreading_layout(dtype, m):
             ran += 1
             assert oracle.rel_l2(colmajor_flat(x), ref) < tol, (bs, rp)
     assert ran >= 2
+
+
+@pytest.mark.parametrize("N", [(512, 64), (64, 512), (512, 32, 32), (32, 32, 512)])
+@pytest.mark.parametrize("prec", [64, 32])
+def test_fused_fft_1024_lines(N, prec):
+    """Lines of 1024 points (radix-8 Stockham passes plus a radix-2 pass in
+    both precisions) along x and along the last dimension."""
+    dtype = np.float64 if prec == 64 else np.float32
+    M = 5000
+    k, f, fhat = rand_problem(len(N), N, M, seed=11 + len(N), dtype=dtype)
+    p = nf.plan_nfft(k, N, m=4, sigma=2.0, precompute=oracle.TENSOR)
+    assert 1024 in p.Ñ
+    y, x = gpu_fwd_adj(p, f, fhat)
+    op = oracle.OraclePlan(k.astype(np.float64), N, m=4, sigma=2.0)
+    tol = TOL64 if prec == 64 else TOL32
+    assert oracle.rel_l2(y, op.forward(f)) < tol
+    assert oracle.rel_l2(colmajor_flat(x), colmajor_flat(op.adjoint(fhat))) < tol
