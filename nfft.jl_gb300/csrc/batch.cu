@@ -169,16 +169,20 @@ __global__ void __launch_bounds__(256) batch_sort_values_kernel(const BatchItem<
   }
 }
 
-// Persistent gather: warps stride over all plans' nodes.
+// Gather: each CTA takes a contiguous chunk of the concatenated (bin-sorted)
+// node ranges, so the nodes an SM visits close in time share their grid
+// neighbourhood in L1 (as in the single-plan gather).
 template <int D, int L, typename T, bool TABLE>
 __global__ void __launch_bounds__(256) batch_gather_kernel(const BatchItem<T>* __restrict__ items, const int64_t* base,
                                                            int n, int64_t total, void* const* __restrict__ ptrs) {
   using C = typename Cplx<T>::type;
   const int lane = threadIdx.x & 31;
-  const int64_t warps_total = int64_t(gridDim.x) * (blockDim.x >> 5);
+  const int64_t chunk = (total + gridDim.x - 1) / gridDim.x;
+  const int64_t lo = int64_t(blockIdx.x) * chunk;
+  const int64_t hi = lo + chunk < total ? lo + chunk : total;
   PolyRegs<D, L, T> P;
   int loaded = -1;
-  for (int64_t q = int64_t(blockIdx.x) * (blockDim.x >> 5) + (threadIdx.x >> 5); q < total; q += warps_total) {
+  for (int64_t q = lo + (threadIdx.x >> 5); q < hi; q += blockDim.x >> 5) {
     const int pi = find_plan(base, n, q);
     const BatchItem<T>& it = items[pi];
     if constexpr (!TABLE) {
@@ -305,9 +309,10 @@ template <int D, int L, typename T, bool TABLE> struct Launch {
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     int64_t ctas = int64_t(std::max(per_sm, 1)) * sms;
     B->spread_ctas = int(std::max<int64_t>(1, std::min<int64_t>(ctas, B->total[B_TASKS])));
-    int gper = 0;
-    NFFT_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&gper, batch_gather_kernel<D, L, T, TABLE>, 256, 0));
-    B->gather_ctas = std::max(1, gper * sms);
+    // gather: CTAs of 8 warps, one contiguous node chunk each (8 nodes per warp
+    // and CTA at least), at most 64 CTAs per SM
+    const int64_t want = (B->total[B_NODES] + 63) / 64;
+    B->gather_ctas = int(std::max<int64_t>(1, std::min<int64_t>(want, int64_t(sms) * 64)));
     return NFFT_OK;
   }
 };
