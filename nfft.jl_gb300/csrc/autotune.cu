@@ -73,7 +73,7 @@ void save_cache() {
 std::vector<std::vector<int64_t>> candidates(const nfft_plan* p) {
   std::vector<std::vector<int64_t>> c;
   if (p->D == 1) {
-    for (int64_t b : {1024, 2048, 4096, 8192}) c.push_back({b, 1, 1, 1});
+    for (int64_t b : {256, 512, 1024, 2048, 4096}) c.push_back({b, 1, 1, 1});
   } else if (p->D == 2) {
     for (auto s : std::vector<std::vector<int64_t>>{{32, 32, 1}, {64, 32, 1}, {64, 64, 1}, {128, 64, 1}, {128, 128, 1}})
       c.push_back({s[0], s[1], s[2], 1});

@@ -46,7 +46,8 @@ int spread_launch(nfft_plan* p, const void* fhat, void* g) {
   T* gp = static_cast<T*>(g);
   if constexpr (D == 1) {
     if (p->prm.compensated) {
-      const size_t smem = sizeof(typename Acc<T, true>::type) * size_t(p->bs[0] + L - 1);
+      const size_t smem = ((sizeof(typename Acc<T, true>::type) * size_t(p->bs[0] + L - 1) + 31) & ~size_t(31)) +
+                          sizeof(T) * size_t(2 * 32 * L + L * (L + 1));
       if (smem > 227 * 1024) {
         set_error("compensated spreading row of %zu bytes does not fit in shared memory; use a smaller blockSize",
                   smem);

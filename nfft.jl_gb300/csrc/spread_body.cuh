@@ -447,8 +447,10 @@ __global__ void __launch_bounds__(kSpreadThreads) spread_pad1_kernel(Geom<T> G, 
 // D = 1, compensated (compensated = 1): one warp per task; lane l owns the
 // padded positions x = l mod 32, so each of a node's L <= 16 taps has exactly
 // one owner lane and the Kahan read-modify-write needs no atomics.  Nodes are
-// visited in bin-sorted order (input order within a tile), the next node's
-// data loaded while the current one is added.
+// visited in bin-sorted order (input order within a tile) in batches of 32:
+// lane l loads node b + l's position and value (broadcast by shuffles) and
+// the batch's window values go to shared memory, the next batch being
+// loaded while the current one is added.
 template <int L, typename T, bool TABLE>
 __global__ void __launch_bounds__(32) spread_line_kahan_kernel(Geom<T> G, Nodes<T> Nd, const int4* __restrict__ tasks,
                                                                 const typename Cplx<T>::type* __restrict__ fhat,
@@ -462,46 +464,72 @@ __global__ void __launch_bounds__(32) spread_line_kahan_kernel(Geom<T> G, Nodes<
   const int4 task = tasks[blockIdx.x];
   const int o0 = task.x * G.bs[0];
   const int P0 = G.bs[0] + L - 1;
+  // window values of two batches (double buffer) and, POLYNOMIAL, the coefficients
+  T* s_w = reinterpret_cast<T*>(smem_raw + ((size_t(P0) * sizeof(A) + 31) & ~size_t(31)));
+  T* s_coef = s_w + 2 * 32 * L;
   const int lane = threadIdx.x;
   {
     A zero;
     memset(&zero, 0, sizeof(A));
     for (int q = lane; q < P0; q += 32) acc[q] = zero;
+    if constexpr (!TABLE)
+      for (int q = lane; q < L * DEG; q += 32) s_coef[q] = __ldg(G.coeffs + q);
   }
   __syncwarp();
-  auto load = [&](int i, int& x0, T& w, C& v) {
-    const int4 nd = __ldg(Nd.node4 + i);
-    x0 = nd.x - o0;
-    const int t = (lane - x0) & 31;
-    w = T(0);
-    if (t < L) {
-      if constexpr (TABLE) {
-        w = __ldg(Nd.wtab + int64_t(i) * L + t);
-      } else {
-        const T tt = __ldg(Nd.frac4 + 4 * int64_t(i)) - T(0.5);
-        const T* c = G.coeffs + t * DEG;
-        w = __ldg(c + DEG - 1);
+  // batch loads: lane l holds node b + l's padded position and value; the
+  // window values of the batch land in s_w[buf]
+  auto load = [&](int b, int buf, int& x0, C& v) {
+    const int n = min(32, task.z - b);
+    x0 = 0;
+    v.x = T(0);
+    v.y = T(0);
+    T fr = T(0);
+    if (lane < n) {
+      const int4 nd = __ldg(Nd.node4 + b + lane);
+      x0 = nd.x - o0;
+      v = __ldg(fhat + nd.w);
+      if constexpr (!TABLE) fr = __ldg(Nd.frac4 + 4 * int64_t(b + lane));
+    }
+    T* w = s_w + buf * 32 * L;
+    if constexpr (TABLE) {
+      for (int q = lane; q < n * L; q += 32) w[q] = __ldg(Nd.wtab + int64_t(b) * L + q);
+    } else {
+      // lane l evaluates the L window values of node b + l
+      const T t = fr - T(0.5);
+      if (lane < n) {
 #pragma unroll
-        for (int q = DEG - 2; q >= 0; --q) w = fma(w, tt, __ldg(c + q));
+        for (int l = 0; l < L; ++l) {
+          const T* c = s_coef + l * DEG;
+          T r = c[DEG - 1];
+#pragma unroll
+          for (int q = DEG - 2; q >= 0; --q) r = fma(r, t, c[q]);
+          w[lane * L + l] = r;
+        }
       }
     }
-    v = __ldg(fhat + nd.w);
   };
   if (task.y < task.z) {
-    int x0;
-    T w;
-    C v;
-    load(task.y, x0, w, v);
-    for (int i = task.y; i < task.z; ++i) {
-      int x0n = 0;
-      T wn = T(0);
-      C vn = v;
-      if (i + 1 < task.z) load(i + 1, x0n, wn, vn);
-      const int t = (lane - x0) & 31;
-      if (t < L) kahan_add<A, T>(acc[x0 + t], w * v.x, w * v.y);
-      x0 = x0n;
-      w = wn;
-      v = vn;
+    int x0c, x0n = 0;
+    C vc, vn;
+    load(task.y, 0, x0c, vc);
+    int buf = 0;
+    for (int b = task.y; b < task.z; b += 32, buf ^= 1) {
+      const int n = min(32, task.z - b);
+      if (b + 32 < task.z) load(b + 32, buf ^ 1, x0n, vn);
+      __syncwarp();
+      const T* w = s_w + buf * 32 * L;
+      for (int s = 0; s < n; ++s) {
+        const int x0 = __shfl_sync(0xFFFFFFFFu, x0c, s);
+        const T vr = __shfl_sync(0xFFFFFFFFu, vc.x, s), vi = __shfl_sync(0xFFFFFFFFu, vc.y, s);
+        const int t = (lane - x0) & 31;
+        if (t < L) {
+          const T wt = w[s * L + t];
+          kahan_add<A, T>(acc[x0 + t], wt * vr, wt * vi);
+        }
+      }
+      __syncwarp();
+      x0c = x0n;
+      vc = vn;
     }
   }
   __syncwarp();
