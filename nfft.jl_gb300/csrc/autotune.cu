@@ -75,7 +75,9 @@ std::vector<std::vector<int64_t>> candidates(const nfft_plan* p) {
   if (p->D == 1) {
     for (int64_t b : {256, 512, 1024, 2048, 4096}) c.push_back({b, 1, 1, 1});
   } else if (p->D == 2) {
-    for (auto s : std::vector<std::vector<int64_t>>{{32, 32, 1}, {64, 32, 1}, {64, 64, 1}, {128, 64, 1}, {128, 128, 1}})
+    // small tiles give small grids enough tasks to fill the GPU
+    for (auto s : std::vector<std::vector<int64_t>>{{8, 8, 1}, {16, 8, 1}, {16, 16, 1}, {32, 16, 1}, {32, 32, 1},
+                                                     {64, 32, 1}, {64, 64, 1}, {128, 64, 1}, {128, 128, 1}})
       c.push_back({s[0], s[1], s[2], 1});
   } else {
     for (auto s : std::vector<std::vector<int64_t>>{{8, 8, 8}, {16, 16, 8}, {16, 16, 16}, {32, 16, 8}, {32, 32, 8},

@@ -137,13 +137,31 @@ void default_block(nfft_plan* p) {
   int64_t def[3][3] = {{1024, 1, 1}, {32, 32, 1}, {16, 16, 16}};
   // compensated 1-D rows hold 16- or 32-byte accumulators and one warp each
   if (p->prm.compensated) def[0][0] = 512;
+  bool user = false;
   for (int d = 0; d < 3; ++d) {
     int64_t b = def[p->D - 1][d];
     if (p->precision == 64 && d == p->D - 1) b = b > 1 ? b / 2 : 1;
-    if (p->prm.block_size[d] > 0 && d < p->D) b = p->prm.block_size[d];
+    if (p->prm.block_size[d] > 0 && d < p->D) {
+      b = p->prm.block_size[d];
+      user = true;
+    }
     if (d >= p->D) b = 1;
     if (b > p->Nt[d]) b = p->Nt[d];
     p->bs[d] = b;
+  }
+  // small grids: halve the largest tile side (down to 8) until there are at
+  // least 4 tiles per SM of a GB300 (152 SMs), so the spreading tasks fill it
+  if (!user) {
+    for (;;) {
+      int64_t nt = 1;
+      int dmax = 0;
+      for (int d = 0; d < p->D; ++d) {
+        nt *= (p->Nt[d] + p->bs[d] - 1) / p->bs[d];
+        if (p->bs[d] > p->bs[dmax]) dmax = d;
+      }
+      if (nt >= 4 * 152 || p->bs[dmax] <= 8) break;
+      p->bs[dmax] /= 2;
+    }
   }
 }
 
