@@ -131,10 +131,11 @@ int64_t lut_size_for(int m) {
 }
 
 void default_block(nfft_plan* p) {
-  // Default tiles (the autotuner refines them): 16^3 (3-D), 32^2 (2-D, two
-  // warps per CTA), 1024 (1-D); the last dimension halved in FP64.  The
+  // Default tiles (the autotuner refines them): 16x8x8 (3-D, the fastest
+  // shape measured on a 256^3 radial set), 32^2 (2-D, two warps per CTA),
+  // 1024 (1-D); the last dimension halved in FP64.  The
   // reference's blockSize keyword overrides them.
-  int64_t def[3][3] = {{1024, 1, 1}, {32, 32, 1}, {16, 16, 16}};
+  int64_t def[3][3] = {{1024, 1, 1}, {32, 32, 1}, {16, 8, 8}};
   // compensated 1-D rows hold 16- or 32-byte accumulators and one warp each
   if (p->prm.compensated) def[0][0] = 512;
   bool user = false;
