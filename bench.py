@@ -574,6 +574,9 @@ CONFIGS = {
                    desc="1-D NFFT fwd+adj, N=2^22, M=2^24 uniform, KB m=5 sigma=2, TENSOR, FP32, compensated"),
     "spiral2d": dict(N=(256, 256), M=65536, m=4, prec=32, nodes="spiral", compensated=False,
                      desc="2-D spiral (32 x 2048) fwd+adj+node gradient, N=256^2, KB m=4 sigma=2, FP32"),
+    "radial3d_fp64": dict(N=(256, 256, 256), M=8192 * 512, m=4, prec=64, nodes="radial", compensated=False,
+                          desc="3D radial koosh-ball NFFT fwd+adj, N=256^3, 8192 spokes x 512 samples, KB m=4 "
+                               "sigma=2, TENSOR, FP64"),
 }
 
 
@@ -589,7 +592,12 @@ def run_config(args):
     rdt = np.float32 if cfg["prec"] == 32 else np.float64
     cd = torch.complex64 if cfg["prec"] == 32 else torch.complex128
     rng = np.random.default_rng(123)
-    k = spiral_nodes(N[0]) if cfg["nodes"] == "spiral" else rng.random((len(N), M)) - 0.5
+    if cfg["nodes"] == "spiral":
+        k = spiral_nodes(N[0])
+    elif cfg["nodes"] == "radial":
+        k = radial_nodes(np.float64)
+    else:
+        k = rng.random((len(N), M)) - 0.5
     k = k.astype(rdt)
     M = k.shape[1]
     f_h = complex_normal(rng, N, np.complex128)
@@ -760,7 +768,7 @@ def main():
                     help="profiling case of the same kernels: N=128^3, 2048 spokes x 256 samples (same node "
                          "density; 134 MB grid, above L2) -- not a bench line")
     ap.add_argument("--workload", default="radial3d",
-                    choices=["radial3d", "batched2d", "plain2d", "line1d", "spiral2d"],
+                    choices=["radial3d", "batched2d", "plain2d", "line1d", "spiral2d", "radial3d_fp64"],
                     help="radial3d: the headline line; the others print extra lines for the other configurations")
     args = ap.parse_args()
     if args.workload == "batched2d":
