@@ -181,20 +181,31 @@ __global__ void __launch_bounds__(256) batch_gather_kernel(const BatchItem<T>* _
   const int64_t lo = int64_t(blockIdx.x) * chunk;
   const int64_t hi = lo + chunk < total ? lo + chunk : total;
   PolyRegs<D, L, T> P;
-  int loaded = -1;
+  // the chunk is contiguous: the plan (and its descriptor) changes only at
+  // plan boundaries, so it is looked up once per plan, not per node
+  // (D = 2 keeps the descriptor in registers; the 3-D node body needs its
+  // registers, so there the fields are read through L1 as needed -- both
+  // measured fastest for their dimension)
+  int64_t pbeg = 0, pend = -1;
+  int pi = 0;
+  Geom<T> G2{};
+  Nodes<T> N2{};
   for (int64_t q = lo + (threadIdx.x >> 5); q < hi; q += blockDim.x >> 5) {
-    const int pi = find_plan(base, n, q);
-    const BatchItem<T>& it = items[pi];
-    if constexpr (!TABLE) {
-      if (pi != loaded) {
-        P.load(it.G.coeffs, lane);
-        loaded = pi;
+    if (q >= pend) {
+      pi = find_plan(base, n, q);
+      pbeg = __ldg(base + pi);
+      pend = __ldg(base + pi + 1);
+      if constexpr (D == 2) {
+        G2 = items[pi].G;
+        N2 = items[pi].Nd;
       }
+      if constexpr (!TABLE) P.load(items[pi].G.coeffs, lane);
     }
-    const Geom<T> G = it.G;
-    const Nodes<T> Nd = it.Nd;
-    interp_node<D, L, T, TABLE>(G, Nd, P, q - __ldg(base + pi), lane,
-                                reinterpret_cast<const C*>(it.grid), static_cast<C*>(ptrs[2 * pi + 1]));
+    const BatchItem<T>& it = items[pi];
+    const C* grid = reinterpret_cast<const C*>(it.grid);
+    C* out = static_cast<C*>(ptrs[2 * pi + 1]);
+    if constexpr (D == 2) interp_node<D, L, T, TABLE>(G2, N2, P, q - pbeg, lane, grid, out);
+    else interp_node<D, L, T, TABLE>(it.G, it.Nd, P, q - pbeg, lane, grid, out);
   }
 }
 
