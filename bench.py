@@ -751,6 +751,118 @@ def run_batched(args):
     return 0
 
 
+def run_toeplitz(args):
+    """--workload toeplitz3d: the Gram operator A^H A of the radial 256^3 plan
+    applied as a Toeplitz convolution (NFFTTools' convolveToeplitzKernel!) on
+    the 512^3 grid -- the fused pruned-FFT path against the cuFFT sequence of
+    the reference (pad, FFT, product, IFFT, crop) and against the forward +
+    adjoint NFFT pair it replaces.  The kernel lambda comes from
+    calculateToeplitzKernel (adjoint NFFT of ones on a 512^3 plan); the timed
+    loop applies lambda / max|lambda| so repeated applications stay finite
+    (same work)."""
+    import torch
+    import nfftgb300 as nf
+    from nfftgb300 import tools
+    dev = torch.device("cuda", torch.cuda.current_device())
+    N = N3
+    k = radial_nodes(np.float32)
+    M = k.shape[1]
+    t0 = time.perf_counter()
+    tz = tools.Toeplitz(N, torch.complex64, dev)
+    lam = tools.calculate_toeplitz_kernel(N, k, m=4, sigma=2.0, toeplitz=tz, precompute=nf.TENSOR)
+    torch.cuda.synchronize()
+    t_kernel = time.perf_counter() - t0
+    torch.cuda.empty_cache()
+    lam_t = lam / lam.abs().max()
+    ref = tools.Toeplitz(N, torch.complex64, dev, fft="cufft")
+    rng = np.random.default_rng(3)
+    x_h = complex_normal(rng, N)
+    x = nf.as_colmajor(x_h, N, torch.complex64, dev)
+    y = x.clone()
+    y2 = x.clone()
+    p = nf.plan_nfft(k, N, m=4, sigma=2.0, precompute=nf.TENSOR)
+    if args.autotune:
+        p.autotune(use_cache=True)
+    fh = torch.empty(M, dtype=torch.complex64, device=dev)
+    xa = nf.empty_image(N, torch.complex64, dev)
+    stream = torch.cuda.current_stream(dev)
+
+    def timed(fn):
+        for _ in range(args.warmup):
+            fn()
+        torch.cuda.synchronize()
+        l0 = nf.kernel_launch_count()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.steps):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) * 1e-3 / args.steps, (nf.kernel_launch_count() - l0) // args.steps
+
+    with ClockSampler(torch.cuda.current_device()) as clk:
+        t_fused, launches = timed(lambda: tz.convolve_(y, lam_t))
+    t_cufft, _ = timed(lambda: ref.convolve_(y2, lam_t))
+    t_pair, _ = timed(lambda: (p.forward_(fh, x), p.adjoint_(xa, fh)))
+    # one application of the true kernel against A^H A through the NFFT pair
+    y.copy_(x)
+    tz.convolve_(y, lam)
+    p.forward_(fh, x)
+    p.adjoint_(xa, fh)
+    y2.copy_(x)
+    ref.convolve_(y2, lam)
+    torch.cuda.synchronize()
+    d_pair = float((y - xa).abs().double().norm() / xa.abs().double().norm())
+    d_cufft = float((y - y2).abs().double().norm() / y2.abs().double().norm())
+    n_img = float(np.prod(N))
+    sc = 8.0
+    design_bytes = 34 * n_img * sc      # pruned passes: x 3, y 6, fused z 16 (incl. lambda 8), y' 6, x' 3
+    compulsory = 10 * n_img * sc        # y in, lambda, y out
+    peak, peak_src = measured_peak_hbm()
+    achieved = design_bytes / t_fused / 1e9
+    line = {
+        "metric": "toeplitz3d: A^H A applications/s (Toeplitz convolution, 256^3 image, 512^3 kernel, FP32)",
+        "value": 1.0 / t_fused, "unit": "applications/s", "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": t_fused * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "Toeplitz Gram operator of the 3-D radial plan: N=256^3, kernel of 8192 spokes x 512 "
+                               "samples (M=4194304) on 512^3, KB m=4 sigma=2",
+                   "l2": "kernel 1.07 GB and grid 1.07 GB exceed L2; no extra flush",
+                   "kernel_seconds": t_kernel},
+        "gpu_launches_per_step": launches,
+        "equivalent_nodes_per_s": M / t_fused,
+        "roofline": {"bound": "hbm", "kernels": "fft4_x_kernel, fft4_lines_kernel, fft4_toeplitz_kernel, "
+                                                "fft4_lines_kernel, fft4_x_kernel (whole application)",
+                     "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "peak_source": peak_src, "algorithmic_bytes": design_bytes,
+                     "compulsory_bytes": compulsory, "traffic": None},
+        "cufft_sequence": {"ms_per_step": t_cufft * 1e3, "speedup_of_value": t_cufft / t_fused,
+                           "rel_diff_vs_fused": d_cufft,
+                           "what": "the reference's sequence on the GPU: zero-fill + corner copy, cuFFT, "
+                                   "product, cuFFT back, crop"},
+        "nfft_pair": {"ms_per_step": t_pair * 1e3, "speedup_of_value": t_pair / t_fused,
+                      "rel_diff_vs_toeplitz": d_pair,
+                      "what": "forward + adjoint NFFT of the same plan (A^H A without the kernel)"},
+        "clocks": clk.summary(),
+    }
+    if not args.no_cpu_baseline:
+        from oracle import oracle
+        threads = oracle.lib().oracle_num_threads()
+        lam_h = lam_t.cpu().numpy()
+        times = []
+        t_start = time.perf_counter()
+        while len(times) < 2 and time.perf_counter() - t_start < 40:
+            ta = time.perf_counter()
+            oracle.convolve_toeplitz(x_h, lam_h, dtype=np.complex64, workers=threads)
+            times.append(time.perf_counter() - ta)
+        per = statistics.median(times)
+        line["cpu_baseline"] = {"value": 1.0 / per, "unit": "applications/s", "cores": threads, "kind": "port",
+                                "sample": f"full workload, {len(times)} applications; oracle restatement of "
+                                          f"convolveToeplitzKernel!, scipy.fft workers={threads}, FP32"}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -768,11 +880,14 @@ def main():
                     help="profiling case of the same kernels: N=128^3, 2048 spokes x 256 samples (same node "
                          "density; 134 MB grid, above L2) -- not a bench line")
     ap.add_argument("--workload", default="radial3d",
-                    choices=["radial3d", "batched2d", "plain2d", "line1d", "spiral2d", "radial3d_fp64"],
+                    choices=["radial3d", "batched2d", "plain2d", "line1d", "spiral2d", "radial3d_fp64",
+                             "toeplitz3d"],
                     help="radial3d: the headline line; the others print extra lines for the other configurations")
     args = ap.parse_args()
     if args.workload == "batched2d":
         return run_batched(args)
+    if args.workload == "toeplitz3d":
+        return run_toeplitz(args)
     if args.workload in CONFIGS:
         return run_config(args)
     if args.small:

@@ -287,6 +287,33 @@ int nfft_dplan_set_stream(nfft_dplan* plan, void* stream);
 int nfft_dplan_forward(nfft_dplan* plan, const void* f, void* fhat);
 int nfft_dplan_adjoint(nfft_dplan* plan, const void* fhat, void* f);
 
+/* Toeplitz tools (NFFTTools/src/Toeplitz.jl): the Gram operator A^H A of a
+ * plan with image size N as a convolution with a kernel lambda on the 2N
+ * grid.  An nfft_toeplitz object owns the 2N-grid workspace and transforms
+ * for one image size N (D <= 3) and precision; fft_mode 0 takes the fused
+ * pruned-FFT path where every 2N_d is a power of two in [64, 1024] and D >= 2
+ * (cuFFT otherwise), 1 always cuFFT.  Arrays are column-major complex T:
+ * y has N points, lambda 2N.  All calls are asynchronous on `stream`. */
+typedef struct nfft_toeplitz nfft_toeplitz;
+int nfft_toeplitz_create(nfft_toeplitz** tz, int precision, int D, const int64_t* N, int fft_mode, void* stream);
+int nfft_toeplitz_destroy(nfft_toeplitz* tz);
+int nfft_toeplitz_set_stream(nfft_toeplitz* tz, void* stream);
+/* 1 when nfft_toeplitz_apply runs the fused path. */
+int nfft_toeplitz_is_fused(const nfft_toeplitz* tz, int* fused);
+/* calculateToeplitzKernel!(lambda, p, tr, fftplan) after nodes!(p, tr)
+ * (Toeplitz.jl:129-135; the allocating form :86-93): lambda =
+ * FFT(fftshift(adjoint(p) * ones(J))).  p: a plan with nodes and size 2N of
+ * the same precision; it runs on its own stream, ordered before this
+ * object's stream. */
+int nfft_toeplitz_kernel(nfft_toeplitz* tz, nfft_plan* plan, void* lambda);
+/* calculateToeplitzKernel_explicit (Toeplitz.jl:142-164): lambda from the
+ * exact sums over the D x M nodes k (T, host or device memory), accumulated
+ * in FP64. */
+int nfft_toeplitz_kernel_explicit(nfft_toeplitz* tz, const void* k, int64_t M, int k_on_device, void* lambda);
+/* convolveToeplitzKernel!(y, lambda) (Toeplitz.jl:230-244), y in place:
+ * y <- crop(IFFT(lambda . FFT(pad(y)))), IFFT normalised by 1/|2N|. */
+int nfft_toeplitz_apply(nfft_toeplitz* tz, const void* lambda, void* y);
+
 /* Wait for the plan's stream. */
 int nfft_sync(nfft_plan* plan);
 

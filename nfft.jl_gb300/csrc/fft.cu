@@ -397,6 +397,57 @@ __global__ void __launch_bounds__(kFftThreads, fft_min_blocks<T, NL, FWD>()) fft
     if (FWD || pos < head || pos >= tail0) *dst = buf[pos * P + w];
 }
 
+// Toeplitz convolution along the last axis with the shared-memory Stockham
+// passes (FP64, and FP32 lines of 1024): pruned load, forward FFT, product
+// with lambda times `scale`, backward FFT, pruned store.
+template <typename T, int NL, int W>
+__global__ void __launch_bounds__(kFftThreads, fft_min_blocks<T, NL, false>()) fft_toeplitz_lines_kernel(
+    LineGeom L, Cx<T>* __restrict__ g, const Cx<T>* __restrict__ lam, T scale, const Cx<T>* __restrict__ tw) {
+  using C = Cx<T>;
+  extern __shared__ __align__(16) unsigned char fft_smem[];
+  C* buf = reinterpret_cast<C*>(fft_smem);
+  constexpr int P = W + 1;
+  const int tile = blockIdx.x % L.tiles_x;
+  const int o = blockIdx.x / L.tiles_x;
+  const int go = L.outer_N > 0 ? wrap_once(o - L.outer_N / 2, L.outer_Nt) : o;
+  const int64_t off = int64_t(go) * L.outer_stride + int64_t(tile) * W;
+  C* base = g + off;
+  const int head = L.n_img - L.n_img / 2;
+  const int tail0 = NL - L.n_img / 2;
+  constexpr int PS = kFftThreads / W;
+  const int w = threadIdx.x % W, p0 = threadIdx.x / W;
+  const int64_t step = int64_t(PS) * L.stride;
+  const C* src = base + w + int64_t(p0) * L.stride;
+#pragma unroll 4
+  for (int pos = p0; pos < NL; pos += PS, src += step) {
+    if (pos < head || pos >= tail0) {
+      cp_async_elem(buf + pos * P + w, src);
+    } else {
+      C z;
+      z.x = T(0);
+      z.y = T(0);
+      buf[pos * P + w] = z;
+    }
+  }
+  cp_async_wait_all();
+  __syncthreads();
+  fft_lines<T, -1, NL, W>(buf, tw);
+  const C* lsrc = lam + off + w + int64_t(p0) * L.stride;
+#pragma unroll 4
+  for (int pos = p0; pos < NL; pos += PS, lsrc += step) {
+    C l = __ldg(lsrc);
+    l.x *= scale;
+    l.y *= scale;
+    buf[pos * P + w] = c_mul(buf[pos * P + w], l);
+  }
+  __syncthreads();
+  fft_lines<T, 1, NL, W>(buf, tw);
+  C* dst = base + w + int64_t(p0) * L.stride;
+#pragma unroll 4
+  for (int pos = p0; pos < NL; pos += PS, dst += step)
+    if (pos < head || pos >= tail0) *dst = buf[pos * P + w];
+}
+
 #ifndef NFFT_FFT_W32
 #define NFFT_FFT_W32 16
 #endif
@@ -641,6 +692,101 @@ __global__ void __launch_bounds__(256, FWD ? 3 : 2) fft4_x_kernel(FftGeom G, Inv
   }
 }
 
+// Toeplitz convolution along the last axis (NFFTTools' convolveToeplitzKernel!):
+// forward FFT of the line's image positions, product with the kernel lambda
+// times `scale`, backward FFT, write back the image positions -- the
+// transformed line never leaves the CTA.  Pass 1 is the forward pass 1 of
+// fft4_lines_kernel.  Pass 2 holds X[k1 + R1 k2] for one k1 after the
+// length-R2 DFT, multiplies by lambda, and runs the backward length-R2 DFT
+// over k2 in the same registers (x[n2 + R2 n1] = sum_k1 e^{+2 pi i k1 n1/R1}
+// e^{+2 pi i k1 n2/N} sum_k2 X[k1 + R1 k2] e^{+2 pi i k2 n2/R2}); it reads and
+// writes the same shared-memory slots, so no barrier separates the two.
+// Pass 3 reads the R1 values of one n2 and finishes with the length-R1 DFT.
+// The kernel product sits in the pass over R2 points; 512 = 32 x 16 keeps
+// that pass at 16 values (32 x 16 the other way spills under two CTAs/SM).
+template <int N> struct ToeSplit {
+  static constexpr int R1 = N == 512 ? 32 : Split4<N>::R1;
+  static constexpr int R2 = N / R1;
+};
+
+template <int NL>
+__global__ void __launch_bounds__(256, 2) fft4_toeplitz_kernel(LineGeom L, float2* __restrict__ g,
+                                                               const float2* __restrict__ lam, float scale,
+                                                               const float2* __restrict__ tw) {
+  using C = float2;
+  constexpr int R1 = ToeSplit<NL>::R1, R2 = ToeSplit<NL>::R2, W = kW4, P = W + 1;
+  extern __shared__ __align__(16) unsigned char fft_smem[];
+  C* y = reinterpret_cast<C*>(fft_smem);
+  const int tile = blockIdx.x % L.tiles_x;
+  const int o = blockIdx.x / L.tiles_x;
+  const int go = L.outer_N > 0 ? wrap_once(o - L.outer_N / 2, L.outer_Nt) : o;
+  const int64_t off = int64_t(go) * L.outer_stride + int64_t(tile) * W;
+  C* base = g + off;
+  const C* lbase = lam + off;
+  const int head = L.n_img - L.n_img / 2, tail0 = NL - L.n_img / 2;
+  constexpr int T1 = W * R2, B1 = (T1 + 255) / 256;
+#pragma unroll
+  for (int b = 0; b < B1; ++b) {
+    const int task = int(threadIdx.x) + b * 256;
+    if (T1 % 256 == 0 || task < T1) {
+      const int w = task % W, n2 = task / W;
+      C v[R1];
+#pragma unroll
+      for (int n1 = 0; n1 < R1; ++n1) {
+        const int n = R2 * n1 + n2;
+        v[n1].x = 0.f;
+        v[n1].y = 0.f;
+        if (n < head || n >= tail0) v[n1] = base[w + int64_t(n) * L.stride];
+      }
+      dft_reg<-1, R1>(v);
+      twiddle4<-1, NL, R1>(v, n2, tw);
+#pragma unroll
+      for (int k1 = 0; k1 < R1; ++k1) y[(n2 * R1 + k1) * P + w] = v[k1];
+    }
+  }
+  __syncthreads();
+  constexpr int T2 = W * R1, B2 = (T2 + 255) / 256;
+#pragma unroll
+  for (int b = 0; b < B2; ++b) {
+    const int task = int(threadIdx.x) + b * 256;
+    if (T2 % 256 == 0 || task < T2) {
+      const int w = task % W, k1 = task / W;
+      C v[R2];
+#pragma unroll
+      for (int n2 = 0; n2 < R2; ++n2) v[n2] = y[(n2 * R1 + k1) * P + w];
+      dft_reg<-1, R2>(v);
+#pragma unroll
+      for (int k2 = 0; k2 < R2; ++k2) {
+        C l = __ldg(lbase + w + int64_t(k1 + R1 * k2) * L.stride);
+        l.x *= scale;
+        l.y *= scale;
+        v[k2] = c_mul(v[k2], l);
+      }
+      dft_reg<1, R2>(v);
+      twiddle4<1, NL, R2>(v, k1, tw);
+#pragma unroll
+      for (int n2 = 0; n2 < R2; ++n2) y[(n2 * R1 + k1) * P + w] = v[n2];
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int b = 0; b < B1; ++b) {
+    const int task = int(threadIdx.x) + b * 256;
+    if (T1 % 256 == 0 || task < T1) {
+      const int w = task % W, n2 = task / W;
+      C v[R1];
+#pragma unroll
+      for (int k1 = 0; k1 < R1; ++k1) v[k1] = y[(n2 * R1 + k1) * P + w];
+      dft_reg<1, R1>(v);
+#pragma unroll
+      for (int n1 = 0; n1 < R1; ++n1) {
+        const int n = R2 * n1 + n2;
+        if (n < head || n >= tail0) base[w + int64_t(n) * L.stride] = v[n1];
+      }
+    }
+  }
+}
+
 template <int N> size_t fft4_smem_bytes() { return size_t(N) * (kW4 + 1) * sizeof(float2); }
 
 FftGeom make_fft_geom(const nfft_plan* p) {
@@ -701,31 +847,34 @@ template <typename T, int NX> int x_pass_t(nfft_plan* p, const void* src, void* 
   return NFFT_OK;
 }
 
-template <typename T, int NL> int line_pass_t(nfft_plan* p, int axis, bool fwd) {
-  using C = Cx<T>;
-  constexpr int W = lines_per_cta<T>();
-  const size_t smem = fft_smem_bytes<NL, T>();
+// Line geometry of a pass along `axis` (1: y, 2: z) with W lines per CTA.
+LineGeom make_line_geom(const nfft_plan* p, int axis, int W, int64_t* outer_count) {
   LineGeom L{};
   L.tiles_x = int(p->Nt[0] / W);
   L.n_img = int(p->N[axis]);
-  int64_t outer_count;
   if (axis == 1) {  // y lines of the image z-slices (D = 3) or of the single plane (D = 2)
     L.stride = p->Nt[0];
     L.outer_stride = p->Nt[0] * p->Nt[1];
     L.outer_N = p->D == 3 ? int(p->N[2]) : 0;
     L.outer_Nt = int(p->Nt[2]);
-    outer_count = p->D == 3 ? p->N[2] : 1;
+    *outer_count = p->D == 3 ? p->N[2] : 1;
   } else {          // z lines of every (x, y)
     L.stride = p->Nt[0] * p->Nt[1];
     L.outer_stride = p->Nt[0];
     L.outer_N = 0;
     L.outer_Nt = int(p->Nt[1]);
-    outer_count = p->Nt[1];
+    *outer_count = p->Nt[1];
   }
+  return L;
+}
+
+template <typename T, int NL> int line_pass_t(nfft_plan* p, int axis, bool fwd) {
+  using C = Cx<T>;
   const C* tw = static_cast<const C*>(p->fft_tw[axis]);
   C* g = static_cast<C*>(p->grid);
+  int64_t outer_count;
   if constexpr (sizeof(T) == 4 && NL <= 512 && NFFT_FFT_FOURSTEP) {
-    L.tiles_x = int(p->Nt[0] / kW4);
+    const LineGeom L = make_line_geom(p, axis, kW4, &outer_count);
     const unsigned blocks4 = unsigned(outer_count * L.tiles_x);
     const size_t smem4 = fft4_smem_bytes<NL>();
     auto kern = fwd ? fft4_lines_kernel<NL, true> : fft4_lines_kernel<NL, false>;
@@ -734,6 +883,9 @@ template <typename T, int NL> int line_pass_t(nfft_plan* p, int axis, bool fwd) 
     NFFT_LAUNCH_CHECK();
     return NFFT_OK;
   }
+  constexpr int W = lines_per_cta<T>();
+  const size_t smem = fft_smem_bytes<NL, T>();
+  const LineGeom L = make_line_geom(p, axis, W, &outer_count);
   const unsigned blocks = unsigned(outer_count * L.tiles_x);
   if (fwd) {
     auto kern = fft_lines_kernel<T, NL, W, true>;
@@ -744,6 +896,34 @@ template <typename T, int NL> int line_pass_t(nfft_plan* p, int axis, bool fwd) 
     if (int rc = set_smem(kern, smem)) return rc;
     kern<<<blocks, kFftThreads, smem, p->stream>>>(L, g, tw);
   }
+  NFFT_LAUNCH_CHECK();
+  return NFFT_OK;
+}
+
+// The fused forward FFT x lambda x backward FFT pass along the last axis.
+template <typename T, int NL> int toeplitz_pass_t(nfft_plan* p, int axis, const void* lam, double scale) {
+  using C = Cx<T>;
+  const C* tw = static_cast<const C*>(p->fft_tw[axis]);
+  C* g = static_cast<C*>(p->grid);
+  const C* l = static_cast<const C*>(lam);
+  int64_t outer_count;
+  if constexpr (sizeof(T) == 4 && NL <= 512 && NFFT_FFT_FOURSTEP) {
+    const LineGeom L = make_line_geom(p, axis, kW4, &outer_count);
+    const unsigned blocks4 = unsigned(outer_count * L.tiles_x);
+    const size_t smem4 = fft4_smem_bytes<NL>();
+    auto kern = fft4_toeplitz_kernel<NL>;
+    if (int rc = set_smem(kern, smem4)) return rc;
+    kern<<<blocks4, 256, smem4, p->stream>>>(L, g, l, float(scale), tw);
+    NFFT_LAUNCH_CHECK();
+    return NFFT_OK;
+  }
+  constexpr int W = lines_per_cta<T>();
+  const size_t smem = fft_smem_bytes<NL, T>();
+  const LineGeom L = make_line_geom(p, axis, W, &outer_count);
+  const unsigned blocks = unsigned(outer_count * L.tiles_x);
+  auto kern = fft_toeplitz_lines_kernel<T, NL, W>;
+  if (int rc = set_smem(kern, smem)) return rc;
+  kern<<<blocks, kFftThreads, smem, p->stream>>>(L, g, l, T(scale), tw);
   NFFT_LAUNCH_CHECK();
   return NFFT_OK;
 }
@@ -770,6 +950,27 @@ template <typename T> int line_pass(nfft_plan* p, int axis, bool fwd) {
   }
   set_error("fused FFT: unsupported length %lld", (long long)p->Nt[axis]);
   return NFFT_ERR_UNSUPPORTED;
+}
+
+template <typename T> int toeplitz_pass(nfft_plan* p, int axis, const void* lam, double scale) {
+  switch (p->Nt[axis]) {
+    case 64: return toeplitz_pass_t<T, 64>(p, axis, lam, scale);
+    case 128: return toeplitz_pass_t<T, 128>(p, axis, lam, scale);
+    case 256: return toeplitz_pass_t<T, 256>(p, axis, lam, scale);
+    case 512: return toeplitz_pass_t<T, 512>(p, axis, lam, scale);
+    case 1024: return toeplitz_pass_t<T, 1024>(p, axis, lam, scale);
+  }
+  set_error("fused FFT: unsupported length %lld", (long long)p->Nt[axis]);
+  return NFFT_ERR_UNSUPPORTED;
+}
+
+template <typename T> int toeplitz_t(nfft_plan* p, const void* lam, double scale, void* y) {
+  int rc = x_pass<T>(p, y, p->grid, true, nullptr);
+  if (!rc && p->D == 3) rc = line_pass<T>(p, 1, true);
+  if (!rc) rc = toeplitz_pass<T>(p, p->D - 1, lam, scale);
+  if (!rc && p->D == 3) rc = line_pass<T>(p, 1, false);
+  if (!rc) rc = x_pass<T>(p, p->grid, y, false, nullptr);
+  return rc;
 }
 
 bool pow2_in_range(int64_t n) { return n >= 64 && n <= 1024 && (n & (n - 1)) == 0; }
@@ -844,6 +1045,17 @@ int fused_adjoint_lines(nfft_plan* p) {
 int fused_adjoint_x(nfft_plan* p, void* f, void* const* f_slot) {
   return p->precision == 32 ? x_pass<float>(p, p->grid, f, false, f_slot)
                             : x_pass<double>(p, p->grid, f, false, f_slot);
+}
+
+// Toeplitz convolution y <- crop(IFFT(lambda . FFT(pad(y)))) on a
+// transform-only plan (N = image, Ntilde = 2N, unit deconvolution factors):
+// forward x pass (pad), forward y pass (D = 3), the fused last-axis pass,
+// backward y pass (D = 3), backward x pass (crop).  The pruned passes place
+// the image centred (wrapped) instead of in the corner of the 2N grid; a
+// circular convolution commutes with that circular shift, so the cropped
+// result equals the corner-placed one.
+int fused_toeplitz(nfft_plan* p, const void* lam, double scale, void* y) {
+  return p->precision == 32 ? toeplitz_t<float>(p, lam, scale, y) : toeplitz_t<double>(p, lam, scale, y);
 }
 
 }  // namespace nfft

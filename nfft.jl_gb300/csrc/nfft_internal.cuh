@@ -189,6 +189,8 @@ int fused_forward_x(nfft_plan* p, const void* f, void* const* f_slot = nullptr);
 int fused_forward_lines(nfft_plan* p);
 int fused_adjoint_lines(nfft_plan* p);
 int fused_adjoint_x(nfft_plan* p, void* f, void* const* f_slot = nullptr);
+// y <- crop(IFFT(scale * lambda . FFT(pad(y)))) on a transform-only plan (N image, Ntilde = 2N)
+int fused_toeplitz(nfft_plan* p, const void* lam, double scale, void* y);
 // gradk.cu
 int launch_grad_nodes(const nfft_plan* p, const void* g, const void* w, void* dk);
 // plain.cu (per-node kernels of the plain path, blocking = 0)

@@ -380,6 +380,95 @@ function batch_mul_adjoint!(fs::Vector{<:CuArray}, b::GB300Batch, fHats::Vector{
   return fs
 end
 
+# ---------------------------------------------------------------- Toeplitz tools
+
+"""
+    GB300Toeplitz(shape, T; fft=:auto)
+
+Workspace of NFFTTools' Toeplitz tools (NFFTTools/src/Toeplitz.jl) for images
+of size `shape` and element type Complex{T}: the 2N grid and transforms that
+`convolveToeplitzKernel!` takes as `fftplan, ifftplan, xOS1, xOS2`.
+`fft=:cufft` forces the cuFFT sequence; `:auto` fuses the pruned transforms
+with the kernel product where every 2N_d is a power of two in [64, 1024].
+The methods below mirror NFFTTools' functions for CuArrays; a maintainer
+hooks them into NFFTTools with, e.g.,
+`NFFTTools.convolveToeplitzKernel!(y::CuArray, λ::CuArray, args...) =
+NFFTGB300.convolveToeplitzKernel!(y, λ)`.
+"""
+mutable struct GB300Toeplitz{T,D}
+  handle::Ptr{Cvoid}
+  shape::NTuple{D,Int}
+end
+
+function GB300Toeplitz(shape::NTuple{D,Int}, ::Type{T}; fft::Symbol=:auto) where {T<:Union{Float32,Float64},D}
+  fft in (:auto, :cufft) || throw(ArgumentError("fft must be :auto or :cufft"))
+  h = Ref{Ptr{Cvoid}}(C_NULL)
+  N = Int64[shape..., ones(Int64, 3 - D)...]
+  check(ccall((:nfft_toeplitz_create, libnfft[]), Cint, (Ref{Ptr{Cvoid}}, Cint, Cint, Ptr{Int64}, Cint, Ptr{Cvoid}),
+              h, T == Float32 ? 32 : 64, D, N, fft == :cufft ? 1 : 0, CUDA.stream().handle))
+  t = GB300Toeplitz{T,D}(h[], shape)
+  finalizer(t) do q
+    q.handle == C_NULL || ccall((:nfft_toeplitz_destroy, libnfft[]), Cint, (Ptr{Cvoid},), q.handle)
+    q.handle = C_NULL
+  end
+  return t
+end
+
+bind_stream!(t::GB300Toeplitz) =
+  check(ccall((:nfft_toeplitz_set_stream, libnfft[]), Cint, (Ptr{Cvoid}, Ptr{Cvoid}), t.handle, CUDA.stream().handle))
+
+function isfused(t::GB300Toeplitz)
+  r = Ref{Cint}(0)
+  check(ccall((:nfft_toeplitz_is_fused, libnfft[]), Cint, (Ptr{Cvoid}, Ref{Cint}), t.handle, r))
+  return r[] == 1
+end
+
+# calculateToeplitzKernel (Toeplitz.jl:86-93)
+function calculateToeplitzKernel(shape::NTuple{D,Int}, tr::AbstractMatrix{T}; m=4, σ=2.0, window=:kaiser_bessel,
+                                 toeplitz::GB300Toeplitz{T,D}=GB300Toeplitz(shape, T), kwargs...) where {T,D}
+  p = AbstractNFFTs.plan_nfft(GB300Backend(), CuArray, Matrix{T}(tr), 2 .* shape; m, σ, window, kwargs...)
+  λ = CuArray{Complex{T}}(undef, 2 .* shape)
+  return calculateToeplitzKernel!(λ, p, toeplitz)
+end
+
+# calculateToeplitzKernel! (Toeplitz.jl:129-135)
+function calculateToeplitzKernel!(λ::CuArray{Complex{T},D}, p::GB300NFFTPlan{T,D}, tr::Matrix{T},
+                                  toeplitz::GB300Toeplitz{T,D}=GB300Toeplitz(p.N .÷ 2, T)) where {T,D}
+  AbstractNFFTs.nodes!(p, tr)
+  return calculateToeplitzKernel!(λ, p, toeplitz)
+end
+
+function calculateToeplitzKernel!(λ::CuArray{Complex{T},D}, p::GB300NFFTPlan{T,D}, t::GB300Toeplitz{T,D}) where {T,D}
+  size(λ) == p.N == 2 .* t.shape || throw(DimensionMismatch("the kernel and the plan must have twice the image size"))
+  bind_stream!(p)
+  bind_stream!(t)
+  check(ccall((:nfft_toeplitz_kernel, libnfft[]), Cint, (Ptr{Cvoid}, Ptr{Cvoid}, CuPtr{Complex{T}}),
+              t.handle, p.handle, λ))
+  return λ
+end
+
+# calculateToeplitzKernel_explicit (Toeplitz.jl:142-164), sums in FP64
+function calculateToeplitzKernel_explicit(shape::NTuple{D,Int}, tr::Matrix{T},
+                                          t::GB300Toeplitz{T,D}=GB300Toeplitz(shape, T)) where {T,D}
+  size(tr, 1) == D || throw(ArgumentError("Nodes x have dimension $(size(tr, 1)) != $D"))
+  λ = CuArray{Complex{T}}(undef, 2 .* shape)
+  kd = CuArray(tr)
+  bind_stream!(t)
+  check(ccall((:nfft_toeplitz_kernel_explicit, libnfft[]), Cint,
+              (Ptr{Cvoid}, CuPtr{T}, Int64, Cint, CuPtr{Complex{T}}), t.handle, kd, size(tr, 2), 1, λ))
+  return λ
+end
+
+# convolveToeplitzKernel! (Toeplitz.jl:230-244), y in place
+function convolveToeplitzKernel!(y::CuArray{Complex{T},D}, λ::CuArray{Complex{T},D},
+                                 t::GB300Toeplitz{T,D}=GB300Toeplitz(size(y), T)) where {T,D}
+  size(λ) == 2 .* size(y) == 2 .* t.shape || throw(DimensionMismatch("the kernel must have twice the image size"))
+  bind_stream!(t)
+  check(ccall((:nfft_toeplitz_apply, libnfft[]), Cint, (Ptr{Cvoid}, CuPtr{Complex{T}}, CuPtr{Complex{T}}),
+              t.handle, λ, y))
+  return y
+end
+
 Base.show(io::IO, p::GB300NFFTPlan) =
   print(io, "GB300NFFTPlan with ", p.J, " sampling points for an input array of size", p.N,
         " and an output array of size", p.NOut, " with dims ", p.dims)

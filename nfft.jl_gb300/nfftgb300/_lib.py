@@ -101,6 +101,13 @@ SIGNATURES = {
     "nfft_dplan_set_stream": (_I, [_P, _P]),
     "nfft_dplan_forward": (_I, [_P, _P, _P]),
     "nfft_dplan_adjoint": (_I, [_P, _P, _P]),
+    "nfft_toeplitz_create": (_I, [ctypes.POINTER(_P), _I, _I, _I64P, _I, _P]),
+    "nfft_toeplitz_destroy": (_I, [_P]),
+    "nfft_toeplitz_set_stream": (_I, [_P, _P]),
+    "nfft_toeplitz_is_fused": (_I, [_P, ctypes.POINTER(ctypes.c_int)]),
+    "nfft_toeplitz_kernel": (_I, [_P, _P, _P]),
+    "nfft_toeplitz_kernel_explicit": (_I, [_P, _P, _I64, _I, _P]),
+    "nfft_toeplitz_apply": (_I, [_P, _P, _P]),
     "nfft_kernel_launch_count": (_I64, []),
     "nfft_status_string": (ctypes.c_char_p, [_I]),
     "nfft_last_error": (ctypes.c_char_p, []),

@@ -450,3 +450,42 @@ def sdc(plan, iters=20):
     workv = plan.adjoint(workf)
     c = np.real(workv.sum()) / np.sum(np.abs(workv) ** 2)
     return (weights * c).astype(rdt)
+
+
+# ----------------------------------------------------------------- Toeplitz
+
+def toeplitz_kernel(shape, tr, m=4, sigma=2.0, window="kaiser_bessel", dtype=np.float64, precompute=TENSOR):
+    """calculateToeplitzKernel (NFFTTools/src/Toeplitz.jl:86-93): FFT of the
+    fftshifted adjoint NFFT of ones on a plan of size 2 .* shape."""
+    shape = tuple(int(n) for n in shape)
+    p = OraclePlan(tr, tuple(2 * n for n in shape), m=m, sigma=sigma, window=window, dtype=dtype,
+                   precompute=precompute)
+    eig = p.adjoint(np.ones(p.M, p.cdtype))
+    return np.fft.fftn(np.fft.fftshift(eig.astype(np.complex128)))
+
+
+def toeplitz_kernel_explicit(shape, tr):
+    """calculateToeplitzKernel_explicit (Toeplitz.jl:142-164): the exact sums
+    getMatrixElement(idx) = sum_j exp(-2 pi i k_j . (shape_os/2 + 1 - idx))
+    = the adjoint NDFT of ones on the 2 .* shape grid, fftshifted and
+    transformed; FP64."""
+    shape_os = tuple(2 * int(n) for n in shape)
+    tr = np.asarray(tr, dtype=np.float64)
+    if tr.ndim == 1:
+        tr = tr.reshape(1, -1)
+    eig = ndft_adjoint(tr, shape_os, np.ones(tr.shape[1], np.complex128))
+    return np.fft.fftn(np.fft.fftshift(eig))
+
+
+def convolve_toeplitz(y, lam, dtype=np.complex128, workers=1):
+    """convolveToeplitzKernel! (Toeplitz.jl:230-244): the image in the corner
+    of a zero grid of lam's size, FFT, product, normalised inverse FFT, crop;
+    computed in ``dtype`` (FP64 by default), returns a new array."""
+    y = np.asarray(y)
+    lam = np.asarray(lam)
+    xos = np.zeros(lam.shape, dtype)
+    xos[tuple(slice(0, n) for n in y.shape)] = y
+    xos = scipy.fft.fftn(xos, workers=workers, overwrite_x=True)
+    xos *= lam
+    xos = scipy.fft.ifftn(xos, workers=workers, overwrite_x=True)
+    return xos[tuple(slice(0, n) for n in y.shape)]

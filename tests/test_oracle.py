@@ -155,3 +155,53 @@ def test_golden(name):
     assert np.array_equal(b["block_start"], z["block_start"])
     assert np.array_equal(b["nodes"], z["block_nodes"])
     assert np.array_equal(b["trunc"], z["trunc"])
+
+
+def _julia_isapprox(a, b, rtol):
+    """Julia's a ≈ b (rtol): norm(a - b) <= rtol * max(norm(a), norm(b))."""
+    a = np.asarray(a, np.complex128).ravel()
+    b = np.asarray(b, np.complex128).ravel()
+    return np.linalg.norm(a - b) <= rtol * max(np.linalg.norm(a), np.linalg.norm(b))
+
+
+@pytest.mark.parametrize("Nx", [32, 33, 64])
+def test_toeplitz_kernel_vs_explicit_2d(Nx):
+    """test/testToeplitz.jl:9-18: calculateToeplitzKernel ≈ the explicit
+    kernel, rtol 1e-6 (2-D, Float64, 1000 nodes)."""
+    rng = np.random.default_rng(Nx)
+    tr = rng.random((2, 1000)) - 0.5
+    kx = oracle.toeplitz_kernel_explicit((Nx, Nx), tr)
+    ka = oracle.toeplitz_kernel((Nx, Nx), tr, m=4, sigma=2.0)
+    assert ka.shape == (2 * Nx, 2 * Nx)
+    assert _julia_isapprox(ka, kx, 1e-6)
+
+
+def test_toeplitz_kernel_fp32_and_gram():
+    """test/testToeplitz.jl:34-52: Float32 kernel ≈ explicit (rtol 1e-5,
+    10000 nodes) and convolveToeplitzKernel!(x, K) ≈ nfft_adjoint(nfft(x))."""
+    rng = np.random.default_rng(7)
+    Nx = 32
+    tr = (rng.random((2, 10000)) - 0.5).astype(np.float32)
+    kx = oracle.toeplitz_kernel_explicit((Nx, Nx), tr)
+    ka = oracle.toeplitz_kernel((Nx, Nx), tr, m=4, sigma=2.0, dtype=np.float32)
+    assert _julia_isapprox(ka, kx, 1e-5)
+    x = (rng.standard_normal((Nx, Nx)) + 1j * rng.standard_normal((Nx, Nx))).astype(np.complex64)
+    p = oracle.OraclePlan(tr, (Nx, Nx), m=4, sigma=2.0, dtype=np.float32)
+    xn = p.adjoint(p.forward(x))
+    assert _julia_isapprox(oracle.convolve_toeplitz(x, ka), xn, 1e-5)
+    # with the exact kernel the Toeplitz product is A^H A up to the NFFT error
+    xd = oracle.ndft_adjoint(tr, (Nx, Nx), oracle.ndft_forward(tr, x))
+    assert oracle.rel_l2(oracle.convolve_toeplitz(x, kx), xd) < 1e-12
+
+
+def test_toeplitz_kernel_rect_and_3d():
+    """test/testToeplitz.jl:58-82: rectangular 2-D (32 x 33) and 3-D kernels,
+    Float32, rtol 1e-5 against the explicit kernel."""
+    rng = np.random.default_rng(9)
+    tr = (rng.random((2, 1000)) - 0.5).astype(np.float32)
+    ka = oracle.toeplitz_kernel((32, 33), tr, dtype=np.float32)
+    assert ka.shape == (64, 66)
+    assert _julia_isapprox(ka, oracle.toeplitz_kernel_explicit((32, 33), tr), 1e-5)
+    tr3 = (rng.random((3, 1000)) - 0.5).astype(np.float32)
+    ka3 = oracle.toeplitz_kernel((32, 32, 32), tr3, dtype=np.float32)
+    assert _julia_isapprox(ka3, oracle.toeplitz_kernel_explicit((32, 32, 32), tr3), 1e-5)
