@@ -764,16 +764,34 @@ def run_toeplitz(args):
     import nfftgb300 as nf
     from nfftgb300 import tools
     dev = torch.device("cuda", torch.cuda.current_device())
-    N = N3
+    N = (256, 256, 256)
     k = radial_nodes(np.float32)
     M = k.shape[1]
     t0 = time.perf_counter()
     tz = tools.Toeplitz(N, torch.complex64, dev)
-    lam = tools.calculate_toeplitz_kernel(N, k, m=4, sigma=2.0, toeplitz=tz, precompute=nf.TENSOR)
+    if args.small:
+        # profiling case: the same 256^3 application with a seeded random
+        # kernel (no 512^3 plan, no comparison arms; ~3.5 GB on the device)
+        g = torch.Generator(device=dev).manual_seed(1)
+        lam = tz.empty_kernel()
+        lam.copy_(torch.randn(lam.shape, dtype=torch.complex64, device=dev, generator=g))
+    else:
+        lam = tools.calculate_toeplitz_kernel(N, k, m=4, sigma=2.0, toeplitz=tz, precompute=nf.TENSOR)
     torch.cuda.synchronize()
     t_kernel = time.perf_counter() - t0
     torch.cuda.empty_cache()
     lam_t = lam / lam.abs().max()
+    if args.small:
+        del lam
+        x = nf.empty_image(N, torch.complex64, dev)
+        x.copy_(torch.randn(N, dtype=torch.complex64, device=dev))
+        y = x.clone()
+        for _ in range(args.warmup + args.steps):
+            tz.convolve_(y, lam_t)
+        torch.cuda.synchronize()
+        print(json.dumps({"workload": "toeplitz3d profiling case (random kernel)", "applications":
+                          args.warmup + args.steps}))
+        return 0
     ref = tools.Toeplitz(N, torch.complex64, dev, fft="cufft")
     rng = np.random.default_rng(3)
     x_h = complex_normal(rng, N)

@@ -182,6 +182,13 @@ template <typename C> __device__ __forceinline__ void cp_async_elem(C* smem, con
 }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
 
+// Pull one 128-byte line toward L2 ahead of its use (no register is held).
+__device__ __forceinline__ void prefetch_l2(const void* p) { asm volatile("prefetch.global.L2 [%0];\n" ::"l"(p)); }
+
+#ifndef NFFT_TOE_PREFETCH
+#define NFFT_TOE_PREFETCH 1
+#endif
+
 // Move the W x n tile elements q = threadIdx.x + i * kFftThreads through
 // registers in batches of up to 8: every load of a batch is issued before
 // its stores, so a thread keeps a batch of global (or shared) loads in flight
@@ -414,6 +421,8 @@ __global__ void __launch_bounds__(kFftThreads, fft_min_blocks<T, NL, false>()) f
   C* base = g + off;
   const int head = L.n_img - L.n_img / 2;
   const int tail0 = NL - L.n_img / 2;
+  if (NFFT_TOE_PREFETCH)
+    for (int r = threadIdx.x; r < NL; r += kFftThreads) prefetch_l2(lam + off + int64_t(r) * L.stride);
   constexpr int PS = kFftThreads / W;
   const int w = threadIdx.x % W, p0 = threadIdx.x / W;
   const int64_t step = int64_t(PS) * L.stride;
@@ -540,6 +549,20 @@ __device__ __forceinline__ void twiddle4(C (&v)[R1], int n2, const C* __restrict
 }
 
 constexpr int kW4 = 16;  // lines per CTA
+
+// Split of the fused Toeplitz pass (fft4_toeplitz_kernel): 512 = 32 x 16, so
+// the 16-point pass carries the twiddles and the kernel product (no spills
+// at two CTAs per SM; 16 x 32 spills).
+#ifndef NFFT_TOE_R1_512
+#define NFFT_TOE_R1_512 32
+#endif
+#ifndef NFFT_TOE_MINB
+#define NFFT_TOE_MINB 2
+#endif
+template <int N> struct ToeSplit {
+  static constexpr int R1 = N == 512 ? NFFT_TOE_R1_512 : Split4<N>::R1;
+  static constexpr int R2 = N / R1;
+};
 
 template <int NL, bool FWD>
 __global__ void __launch_bounds__(256, FWD ? 3 : 2) fft4_lines_kernel(LineGeom L, float2* __restrict__ g,
@@ -695,26 +718,26 @@ __global__ void __launch_bounds__(256, FWD ? 3 : 2) fft4_x_kernel(FftGeom G, Inv
 // Toeplitz convolution along the last axis (NFFTTools' convolveToeplitzKernel!):
 // forward FFT of the line's image positions, product with the kernel lambda
 // times `scale`, backward FFT, write back the image positions -- the
-// transformed line never leaves the CTA.  Pass 1 is the forward pass 1 of
-// fft4_lines_kernel.  Pass 2 holds X[k1 + R1 k2] for one k1 after the
-// length-R2 DFT, multiplies by lambda, and runs the backward length-R2 DFT
-// over k2 in the same registers (x[n2 + R2 n1] = sum_k1 e^{+2 pi i k1 n1/R1}
-// e^{+2 pi i k1 n2/N} sum_k2 X[k1 + R1 k2] e^{+2 pi i k2 n2/R2}); it reads and
-// writes the same shared-memory slots, so no barrier separates the two.
-// Pass 3 reads the R1 values of one n2 and finishes with the length-R1 DFT.
-// The kernel product sits in the pass over R2 points; 512 = 32 x 16 keeps
-// that pass at 16 values (32 x 16 the other way spills under two CTAs/SM).
-template <int N> struct ToeSplit {
-  static constexpr int R1 = N == 512 ? 32 : Split4<N>::R1;
-  static constexpr int R2 = N / R1;
-};
-
+// transformed line never leaves the CTA.  N = R1 R2 with n = R2 n1 + n2 and
+// k = k1 + R1 k2:
+//   pass 1 (thread per n2): length-R1 DFT over n1 of the image positions;
+//   pass 2 (thread per k1): twiddle e^{-2 pi i n2 k1/N}, length-R2 DFT over
+//     n2 (now X[k1 + R1 k2]), product with lambda, backward length-R2 DFT
+//     over k2, twiddle e^{+2 pi i k1 n2/N} -- the same table entries as the
+//     forward twiddle, loaded once; it reads and writes the same shared-memory
+//     slots, so no barrier separates the halves;
+//   pass 3 (thread per n2): backward length-R1 DFT, image positions written.
+// Both twiddles sit in the pass over R2 points, which keeps the pass over R1
+// points free of table loads.  The image occupies positions [0, N/4) and
+// [3N/4, N) (the grid is twice the image), i.e. n1 in [0, R1/4) and
+// [3R1/4, R1) -- compile-time in the unrolled loops.
 template <int NL>
-__global__ void __launch_bounds__(256, 2) fft4_toeplitz_kernel(LineGeom L, float2* __restrict__ g,
-                                                               const float2* __restrict__ lam, float scale,
-                                                               const float2* __restrict__ tw) {
+__global__ void __launch_bounds__(256, NFFT_TOE_MINB) fft4_toeplitz_kernel(LineGeom L, float2* __restrict__ g,
+                                                                           const float2* __restrict__ lam, float scale,
+                                                                           const float2* __restrict__ tw) {
   using C = float2;
   constexpr int R1 = ToeSplit<NL>::R1, R2 = ToeSplit<NL>::R2, W = kW4, P = W + 1;
+  static_assert(R1 % 4 == 0, "image quarter of the R1 index");
   extern __shared__ __align__(16) unsigned char fft_smem[];
   C* y = reinterpret_cast<C*>(fft_smem);
   const int tile = blockIdx.x % L.tiles_x;
@@ -723,7 +746,12 @@ __global__ void __launch_bounds__(256, 2) fft4_toeplitz_kernel(LineGeom L, float
   const int64_t off = int64_t(go) * L.outer_stride + int64_t(tile) * W;
   C* base = g + off;
   const C* lbase = lam + off;
-  const int head = L.n_img - L.n_img / 2, tail0 = NL - L.n_img / 2;
+  if (NFFT_TOE_PREFETCH && NL >= 512) {
+    // the CTA's kernel tile (NL rows of W values = one 128-byte line each)
+    // streams into L2 while pass 1 loads and transforms; pass 2 reads it
+    // there (measured: 512-point lines 4 % faster, 256-point lines slower)
+    for (int r = threadIdx.x; r < NL; r += 256) prefetch_l2(lbase + int64_t(r) * L.stride);
+  }
   constexpr int T1 = W * R2, B1 = (T1 + 255) / 256;
 #pragma unroll
   for (int b = 0; b < B1; ++b) {
@@ -733,13 +761,11 @@ __global__ void __launch_bounds__(256, 2) fft4_toeplitz_kernel(LineGeom L, float
       C v[R1];
 #pragma unroll
       for (int n1 = 0; n1 < R1; ++n1) {
-        const int n = R2 * n1 + n2;
         v[n1].x = 0.f;
         v[n1].y = 0.f;
-        if (n < head || n >= tail0) v[n1] = base[w + int64_t(n) * L.stride];
+        if (n1 < R1 / 4 || n1 >= 3 * R1 / 4) v[n1] = base[w + int64_t(R2 * n1 + n2) * L.stride];
       }
       dft_reg<-1, R1>(v);
-      twiddle4<-1, NL, R1>(v, n2, tw);
 #pragma unroll
       for (int k1 = 0; k1 < R1; ++k1) y[(n2 * R1 + k1) * P + w] = v[k1];
     }
@@ -751,9 +777,13 @@ __global__ void __launch_bounds__(256, 2) fft4_toeplitz_kernel(LineGeom L, float
     const int task = int(threadIdx.x) + b * 256;
     if (T2 % 256 == 0 || task < T2) {
       const int w = task % W, k1 = task / W;
-      C v[R2];
+      C v[R2], t[R2];
+      t[0].x = 1.f;
+      t[0].y = 0.f;
 #pragma unroll
-      for (int n2 = 0; n2 < R2; ++n2) v[n2] = y[(n2 * R1 + k1) * P + w];
+      for (int n2 = 1; n2 < R2; ++n2) t[n2] = __ldg(tw + ((n2 * k1) & (NL - 1)));
+#pragma unroll
+      for (int n2 = 0; n2 < R2; ++n2) v[n2] = c_mul(y[(n2 * R1 + k1) * P + w], t[n2]);
       dft_reg<-1, R2>(v);
 #pragma unroll
       for (int k2 = 0; k2 < R2; ++k2) {
@@ -763,9 +793,12 @@ __global__ void __launch_bounds__(256, 2) fft4_toeplitz_kernel(LineGeom L, float
         v[k2] = c_mul(v[k2], l);
       }
       dft_reg<1, R2>(v);
-      twiddle4<1, NL, R2>(v, k1, tw);
 #pragma unroll
-      for (int n2 = 0; n2 < R2; ++n2) y[(n2 * R1 + k1) * P + w] = v[n2];
+      for (int n2 = 0; n2 < R2; ++n2) {
+        C c = t[n2];
+        c.y = -c.y;
+        y[(n2 * R1 + k1) * P + w] = c_mul(v[n2], c);
+      }
     }
   }
   __syncthreads();
@@ -779,10 +812,8 @@ __global__ void __launch_bounds__(256, 2) fft4_toeplitz_kernel(LineGeom L, float
       for (int k1 = 0; k1 < R1; ++k1) v[k1] = y[(n2 * R1 + k1) * P + w];
       dft_reg<1, R1>(v);
 #pragma unroll
-      for (int n1 = 0; n1 < R1; ++n1) {
-        const int n = R2 * n1 + n2;
-        if (n < head || n >= tail0) base[w + int64_t(n) * L.stride] = v[n1];
-      }
+      for (int n1 = 0; n1 < R1; ++n1)
+        if (n1 < R1 / 4 || n1 >= 3 * R1 / 4) base[w + int64_t(R2 * n1 + n2) * L.stride] = v[n1];
     }
   }
 }
