@@ -314,6 +314,36 @@ int nfft_toeplitz_kernel_explicit(nfft_toeplitz* tz, const void* k, int64_t M, i
  * y <- crop(IFFT(lambda . FFT(pad(y)))), IFFT normalised by 1/|2N|. */
 int nfft_toeplitz_apply(nfft_toeplitz* tz, const void* lambda, void* y);
 
+/* Direct (exact) transforms of src/direct.jl on the device, sums in FP64:
+ * NDFTPlan (:99-151), NDCTPlan (:153-199), NDSTPlan (:202-249), NNDFTPlan
+ * (:252-287).  N: the plan's N (D <= 4; the NDST's image is N - 1 per
+ * dimension; the NNDFT's N[0] is the number of points y).  k: D x M nodes,
+ * y: D x N[0] points (NNDFT), both T on the device.  adjoint = 0: image ->
+ * M node values (NDFT/NNDFT sign -1); 1: the adjoint (sign +1) or, for the
+ * NDCT/NDST, the transpose.  complex_data: interleaved complex T in and out
+ * (required for NDFT/NNDFT), else real T.  Asynchronous on `stream`. */
+enum { NFFT_NDFT = 0, NFFT_NDCT = 1, NFFT_NDST = 2, NFFT_NNDFT = 3 };
+int nfft_direct(int kind, int precision, int D, const int64_t* N, int64_t M, const void* k, const void* y,
+                int adjoint, int complex_data, const void* in, void* out, void* stream);
+
+/* NFCT / NFST plans (the AbstractNFCTPlan / AbstractNFSTPlan types of
+ * AbstractNFFTs/src/interface.jl:73-90; NFFT.jl itself computes them only
+ * directly, src/direct.jl:153-249): kind NFFT_NDCT or NFFT_NDST, real data of
+ * type T.  NFCT: f has N points, n_d = 0..N_d-1; NFST: f has N - 1 points,
+ * n_d = 1..N_d-1 (size_in = N .- 1, as NDSTPlan).  Computed by the NFFT of
+ * size 2N (params as for nfft_plan_create) of the even / odd extension of f;
+ * the transpose folds the adjoint NFFT.  Nodes as for nfft_set_nodes. */
+typedef struct nfft_tplan nfft_tplan;
+int nfft_tplan_create(nfft_tplan** plan, int kind, int precision, int D, const int64_t* N, int64_t M,
+                      const nfft_params* params, void* stream);
+int nfft_tplan_destroy(nfft_tplan* plan);
+int nfft_tplan_set_stream(nfft_tplan* plan, void* stream);
+int nfft_tplan_set_nodes(nfft_tplan* plan, const void* k, int k_on_device);
+/* mul!(fHat, p, f): real f -> real fHat (M) */
+int nfft_tplan_forward(nfft_tplan* plan, const void* f, void* fhat);
+/* mul!(f, transpose(p), fHat): real fHat (M) -> real f */
+int nfft_tplan_transpose(nfft_tplan* plan, const void* fhat, void* f);
+
 /* Wait for the plan's stream. */
 int nfft_sync(nfft_plan* plan);
 

@@ -469,6 +469,103 @@ function convolveToeplitzKernel!(y::CuArray{Complex{T},D}, λ::CuArray{Complex{T
   return y
 end
 
+# ---------------------------------------------------------------- NFCT / NFST plans
+
+const KIND_NDFT, KIND_NDCT, KIND_NDST, KIND_NNDFT = 0, 1, 2, 3
+
+"""
+    plan_nfct(CuArray, k, N; m, σ, window, ...)   /   plan_nfst(CuArray, k, N; ...)
+
+NFCT / NFST plans (AbstractNFCTPlan / AbstractNFSTPlan) on the GPU NFFT of
+size 2N of the even / odd extension (`nfft_tplan_*`); real data of type T.
+The NFST input has N .- 1 points, as NDSTPlan.
+"""
+mutable struct GB300TrigPlan{T,D,KIND}
+  handle::Ptr{Cvoid}
+  N::NTuple{D,Int}
+  J::Int
+  k::Matrix{T}
+end
+const GB300NFCTPlan{T,D} = GB300TrigPlan{T,D,KIND_NDCT}
+const GB300NFSTPlan{T,D} = GB300TrigPlan{T,D,KIND_NDST}
+
+function trig_plan(kind::Int, k::Matrix{T}, N::NTuple{D,Int}; window::Symbol=:kaiser_bessel,
+                   precompute=AbstractNFFTs.POLYNOMIAL, blocking::Bool=true, kwargs...) where {T,D}
+  size(k, 1) == D || throw(ArgumentError("Nodes x have dimension $(size(k,1)) != $D"))
+  m, σ, reltol = AbstractNFFTs.accuracyParams(; kwargs...)
+  cp = CParams(m, σ, WINDOWS[window], Int(precompute), blocking, false, false, (0, 0, 0), 0, 0)
+  Nc = Int64[N...; ones(Int64, 3 - D)]
+  h = Ref{Ptr{Cvoid}}(C_NULL)
+  check(ccall((:nfft_tplan_create, libnfft[]), Cint,
+              (Ref{Ptr{Cvoid}}, Cint, Cint, Cint, Ptr{Int64}, Int64, Ref{CParams}, Ptr{Cvoid}),
+              h, kind, T == Float32 ? 32 : 64, D, Nc, size(k, 2), cp, CUDA.stream().handle))
+  p = GB300TrigPlan{T,D,kind}(h[], N, size(k, 2), k)
+  finalizer(p) do q
+    q.handle == C_NULL || ccall((:nfft_tplan_destroy, libnfft[]), Cint, (Ptr{Cvoid},), q.handle)
+    q.handle = C_NULL
+  end
+  AbstractNFFTs.nodes!(p, k)
+  return p
+end
+
+AbstractNFFTs.plan_nfct(::GB300Backend, ::Type{<:CuArray}, k::Matrix{T}, N::NTuple{D,Int}, rest...;
+                        kwargs...) where {T<:Union{Float32,Float64},D} = trig_plan(KIND_NDCT, k, N; kwargs...)
+AbstractNFFTs.plan_nfst(::GB300Backend, ::Type{<:CuArray}, k::Matrix{T}, N::NTuple{D,Int}, rest...;
+                        kwargs...) where {T<:Union{Float32,Float64},D} = trig_plan(KIND_NDST, k, N; kwargs...)
+
+AbstractNFFTs.size_in(p::GB300TrigPlan{T,D,KIND_NDCT}) where {T,D} = p.N
+AbstractNFFTs.size_in(p::GB300TrigPlan{T,D,KIND_NDST}) where {T,D} = p.N .- 1
+AbstractNFFTs.size_out(p::GB300TrigPlan) = (p.J,)
+
+bind_stream!(p::GB300TrigPlan) =
+  check(ccall((:nfft_tplan_set_stream, libnfft[]), Cint, (Ptr{Cvoid}, Ptr{Cvoid}), p.handle, CUDA.stream().handle))
+
+function AbstractNFFTs.nodes!(p::GB300TrigPlan{T}, k::Matrix{T}) where {T}
+  size(k) == size(p.k) || throw(DimensionMismatch("nodes must be $(size(p.k))"))
+  bind_stream!(p)
+  check(ccall((:nfft_tplan_set_nodes, libnfft[]), Cint, (Ptr{Cvoid}, Ptr{T}, Cint), p.handle, k, 0))
+  p.k = k
+  return p
+end
+
+function LinearAlgebra.mul!(fHat::CuVector{T}, p::GB300TrigPlan{T,D}, f::CuArray{T,D}) where {T,D}
+  size(f) == size_in(p) && length(fHat) == p.J || throw(DimensionMismatch("Data is not consistent with the plan"))
+  bind_stream!(p)
+  check(ccall((:nfft_tplan_forward, libnfft[]), Cint, (Ptr{Cvoid}, CuPtr{T}, CuPtr{T}), p.handle, f, fHat))
+  return fHat
+end
+
+function LinearAlgebra.mul!(f::CuArray{T,D}, pl::Transpose{T,<:GB300TrigPlan{T,D}}, fHat::CuVector{T}) where {T,D}
+  p = pl.parent
+  size(f) == size_in(p) && length(fHat) == p.J || throw(DimensionMismatch("Data is not consistent with the plan"))
+  bind_stream!(p)
+  check(ccall((:nfft_tplan_transpose, libnfft[]), Cint, (Ptr{Cvoid}, CuPtr{T}, CuPtr{T}), p.handle, fHat, f))
+  return f
+end
+
+# ---------------------------------------------------------------- direct transforms (src/direct.jl)
+
+"""
+    direct_mul!(out, kind, k, N, in; adjoint=false, y=nothing)
+
+Exact NDFT / NDCT / NDST / NNDFT products on the GPU (`nfft_direct`, sums in
+FP64): `kind` is KIND_NDFT, KIND_NDCT, KIND_NDST or KIND_NNDFT; `k` the D x J
+nodes, `N` the plan size (NNDFT: `(size(y, 2),)`), `adjoint=true` for the
+adjoint / transpose.
+"""
+function direct_mul!(out::CuArray, kind::Int, k::CuMatrix{T}, N::NTuple{D,Int}, x::CuArray;
+                     adjoint::Bool=false, y::Union{Nothing,CuMatrix{T}}=nothing) where {T,D}
+  cplx = eltype(x) <: Complex
+  Nc = Int64[N...; ones(Int64, 4 - D)]
+  yp = y === nothing ? CuPtr{T}(0) : pointer(y)
+  check(ccall((:nfft_direct, libnfft[]), Cint,
+              (Cint, Cint, Cint, Ptr{Int64}, Int64, CuPtr{T}, CuPtr{T}, Cint, Cint, CuPtr{Cvoid}, CuPtr{Cvoid},
+               Ptr{Cvoid}),
+              kind, T == Float32 ? 32 : 64, size(k, 1), Nc, size(k, 2), k, yp, adjoint, cplx, x, out,
+              CUDA.stream().handle))
+  return out
+end
+
 Base.show(io::IO, p::GB300NFFTPlan) =
   print(io, "GB300NFFTPlan with ", p.J, " sampling points for an input array of size", p.N,
         " and an output array of size", p.NOut, " with dims ", p.dims)

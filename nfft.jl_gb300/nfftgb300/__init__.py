@@ -9,4 +9,7 @@ from .plan import (  # noqa: F401
     convolve_transpose_, deconvolve_, deconvolve_transpose_, empty_image, kernel_launch_count, mul_, nfft,
     nfft_adjoint, GB300DirectionalPlan, NFFTBatch, nodes_, params_to_reltol, plan_nfft, reltol_to_params, size_in,
     size_out)
+from .trig import (  # noqa: F401
+    GB300NFCTPlan, GB300NFSTPlan, NDCTPlan, NDFTPlan, NDSTPlan, NNDFTPlan, ndct, ndct_transposed, ndft, ndft_adjoint,
+    nfct, nfct_transpose, nfst, nfst_transpose, plan_nfct, plan_nfst)
 from ._lib import LIB_PATH, exported_symbols, load  # noqa: F401

@@ -108,6 +108,13 @@ SIGNATURES = {
     "nfft_toeplitz_kernel": (_I, [_P, _P, _P]),
     "nfft_toeplitz_kernel_explicit": (_I, [_P, _P, _I64, _I, _P]),
     "nfft_toeplitz_apply": (_I, [_P, _P, _P]),
+    "nfft_direct": (_I, [_I, _I, _I, _I64P, _I64, _P, _P, _I, _I, _P, _P, _P]),
+    "nfft_tplan_create": (_I, [ctypes.POINTER(_P), _I, _I, _I, _I64P, _I64, ctypes.POINTER(nfft_params), _P]),
+    "nfft_tplan_destroy": (_I, [_P]),
+    "nfft_tplan_set_stream": (_I, [_P, _P]),
+    "nfft_tplan_set_nodes": (_I, [_P, _P, _I]),
+    "nfft_tplan_forward": (_I, [_P, _P, _P]),
+    "nfft_tplan_transpose": (_I, [_P, _P, _P]),
     "nfft_kernel_launch_count": (_I64, []),
     "nfft_status_string": (ctypes.c_char_p, [_I]),
     "nfft_last_error": (ctypes.c_char_p, []),

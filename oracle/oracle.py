@@ -489,3 +489,90 @@ def convolve_toeplitz(y, lam, dtype=np.complex128, workers=1):
     xos *= lam
     xos = scipy.fft.ifftn(xos, workers=workers, overwrite_x=True)
     return xos[tuple(slice(0, n) for n in y.shape)]
+
+
+# ------------------------------------------------- NDCT / NDST / NNDFT
+
+def _trig_factors(k, N, fun, shift):
+    """Per-dimension factor matrices fun(2 pi k_dj (n + shift)), n = 0..N_d-1."""
+    k = np.asarray(k, dtype=np.float64)
+    if k.ndim == 1:
+        k = k.reshape(1, -1)
+    return [fun(2.0 * np.pi * np.outer(k[d], np.arange(N[d], dtype=np.float64) + shift)) for d in range(len(N))]
+
+
+def _contract(mats, f):
+    """g_j = sum_n f[n] prod_d mats[d][j, n_d] for f of logical shape N."""
+    D = len(mats)
+    letters = "abcd"[:D]
+    expr = ",".join(f"j{c}" for c in letters) + "," + letters + "->j"
+    return np.einsum(expr, *mats, f, optimize=True)
+
+
+def _contract_t(mats, v):
+    """f[n] = sum_j v_j prod_d mats[d][j, n_d]."""
+    D = len(mats)
+    letters = "abcd"[:D]
+    expr = ",".join(f"j{c}" for c in letters) + ",j->" + letters
+    return np.einsum(expr, *mats, v, optimize=True)
+
+
+def ndct_forward(k, f):
+    """NDCTPlan * f (src/direct.jl:153-174): fHat_j = sum_n f_n prod_d
+    cos(2 pi k_dj n_d), n_d = 0..N_d-1; FP64."""
+    f = np.asarray(f)
+    return _contract(_trig_factors(k, f.shape, np.cos, 0.0), f.astype(np.result_type(f, np.float64)))
+
+
+def ndct_transpose(k, N, fhat):
+    """transpose(NDCTPlan) * fHat (src/direct.jl:177-199)."""
+    fhat = np.asarray(fhat)
+    return _contract_t(_trig_factors(k, tuple(N), np.cos, 0.0), fhat.astype(np.result_type(fhat, np.float64)))
+
+
+def ndst_forward(k, f):
+    """NDSTPlan * f (src/direct.jl:202-224): the input has N - 1 points per
+    dimension, n_d = 1..N_d-1, factors sin(2 pi k_dj n_d); FP64."""
+    f = np.asarray(f)
+    return _contract(_trig_factors(k, f.shape, np.sin, 1.0), f.astype(np.result_type(f, np.float64)))
+
+
+def ndst_transpose(k, N, fhat):
+    """transpose(NDSTPlan) * fHat (src/direct.jl:227-249); N is the plan
+    size, the output has N - 1 points per dimension."""
+    fhat = np.asarray(fhat)
+    Nm = tuple(int(n) - 1 for n in N)
+    return _contract_t(_trig_factors(k, Nm, np.sin, 1.0), fhat.astype(np.result_type(fhat, np.float64)))
+
+
+def nndft_forward(k, y, f):
+    """NNDFTPlan * f (src/direct.jl:252-268): fHat_j = sum_l f_l
+    exp(-2 pi i k_j . y_l); FP64."""
+    k = np.atleast_2d(np.asarray(k, dtype=np.float64))
+    y = np.atleast_2d(np.asarray(y, dtype=np.float64))
+    return np.exp(-2j * np.pi * (k.T @ y)) @ np.asarray(f, dtype=np.complex128)
+
+
+def nndft_adjoint(k, y, fhat):
+    """adjoint(NNDFTPlan) * fHat (src/direct.jl:270-287)."""
+    k = np.atleast_2d(np.asarray(k, dtype=np.float64))
+    y = np.atleast_2d(np.asarray(y, dtype=np.float64))
+    return np.exp(2j * np.pi * (y.T @ k)) @ np.asarray(fhat, dtype=np.complex128)
+
+
+def ndft_forward_sep(k, f):
+    """The NDFT of ndft_forward by per-dimension phase matrices (any D <= 4):
+    exp(-2 pi i k_dj (n_d - N_d div 2)); FP64."""
+    f = np.asarray(f)
+    N = f.shape
+    k = np.atleast_2d(np.asarray(k, dtype=np.float64))
+    mats = [np.exp(-2j * np.pi * np.outer(k[d], np.arange(N[d]) - N[d] // 2)) for d in range(len(N))]
+    return _contract(mats, f.astype(np.complex128))
+
+
+def ndft_adjoint_sep(k, N, fhat):
+    """The adjoint NDFT of ndft_adjoint by per-dimension phase matrices."""
+    N = tuple(int(n) for n in N)
+    k = np.atleast_2d(np.asarray(k, dtype=np.float64))
+    mats = [np.exp(2j * np.pi * np.outer(k[d], np.arange(N[d]) - N[d] // 2)) for d in range(len(N))]
+    return _contract_t(mats, np.asarray(fhat, dtype=np.complex128))

@@ -205,3 +205,54 @@ def test_toeplitz_kernel_rect_and_3d():
     tr3 = (rng.random((3, 1000)) - 0.5).astype(np.float32)
     ka3 = oracle.toeplitz_kernel((32, 32, 32), tr3, dtype=np.float32)
     assert _julia_isapprox(ka3, oracle.toeplitz_kernel_explicit((32, 32, 32), tr3), 1e-5)
+
+
+def test_ndct_ndst_known_answers():
+    """NDCT / NDST at equispaced nodes are type-I DCT / DST (scipy.fft, an
+    independent implementation): with k_j = j / (2 (N - 1)),
+    sum_n f_n cos(pi j n / (N - 1)) = (DCT-I(f)_j + f_0 + (-1)^j f_{N-1}) / 2;
+    with k_j = (j + 1) / (2 N) and the N - 1 inputs of an NDST plan of size N,
+    sum_n f_n sin(pi (j + 1) n / N) = DST-I(f)_j / 2."""
+    import scipy.fft as sf
+    rng = np.random.default_rng(0)
+    N = 33
+    f = rng.standard_normal(N)
+    k = np.arange(N) / (2.0 * (N - 1))
+    j = np.arange(N)
+    ref = (sf.dct(f, type=1) + f[0] + (-1.0) ** j * f[-1]) / 2
+    np.testing.assert_allclose(oracle.ndct_forward(k, f), ref, rtol=1e-12, atol=1e-12)
+    Nst = 17
+    g = rng.standard_normal(Nst - 1)
+    ks = (np.arange(Nst - 1) + 1) / (2.0 * Nst)
+    np.testing.assert_allclose(oracle.ndst_forward(ks, g), sf.dst(g, type=1) / 2, rtol=1e-12, atol=1e-12)
+    # 2-D: separable products of the 1-D cases
+    f2 = rng.standard_normal((N, 9))
+    k2 = np.stack([k[:9], np.arange(9) / 16.0])
+    direct = np.array([sum(f2[a, b] * np.cos(2 * np.pi * k2[0, q] * a) * np.cos(2 * np.pi * k2[1, q] * b)
+                           for a in range(N) for b in range(9)) for q in range(9)])
+    np.testing.assert_allclose(oracle.ndct_forward(k2, f2), direct, rtol=1e-12, atol=1e-12)
+
+
+def test_direct_transposes_and_ndft_forms():
+    rng = np.random.default_rng(1)
+    for N in [(12,), (6, 7), (5, 4, 6), (3, 4, 3, 2)]:
+        D = len(N)
+        k = rng.random((D, 30)) * 0.5
+        f = rng.standard_normal(N)
+        v = rng.standard_normal(30)
+        assert abs(oracle.ndct_forward(k, f) @ v - np.sum(f * oracle.ndct_transpose(k, N, v))) < 1e-10
+        Np = tuple(n + 1 for n in N)
+        assert abs(oracle.ndst_forward(k, f) @ v - np.sum(f * oracle.ndst_transpose(k, Np, v))) < 1e-10
+        kc = rng.random((D, 30)) - 0.5
+        fc = f + 1j * rng.standard_normal(N)
+        if D <= 3:
+            np.testing.assert_allclose(oracle.ndft_forward_sep(kc, fc), oracle.ndft_forward(kc, fc), rtol=1e-12)
+            np.testing.assert_allclose(oracle.ndft_adjoint_sep(kc, N, v), oracle.ndft_adjoint(kc, N, v),
+                                       rtol=1e-12, atol=1e-12)
+        # NNDFT on the integer points n - N div 2 is the NDFT
+        grids = np.meshgrid(*[np.arange(n) - n // 2 for n in N], indexing="ij")
+        y = np.stack([g.ravel(order="F") for g in grids]).astype(np.float64)
+        np.testing.assert_allclose(oracle.nndft_forward(kc, y, fc.ravel(order="F")),
+                                   oracle.ndft_forward_sep(kc, fc), rtol=1e-11)
+        np.testing.assert_allclose(oracle.nndft_adjoint(kc, y, v),
+                                   oracle.ndft_adjoint_sep(kc, N, v).ravel(order="F"), rtol=1e-11, atol=1e-11)
