@@ -881,6 +881,143 @@ def run_toeplitz(args):
     return 0
 
 
+def run_extras(args):
+    """--workload extras: one JSON line per widened row, each measured on the
+    device with CUDA events (W warm-up, K timed steps):
+      windows x precompute modes of the 256^3 radial plan (fwd+adj, rel. error
+      vs the FP64 NDFT on node / frequency subsets);
+      a directional plan: 2-D NFFTs (dims 1:2) of the 64 slices of a
+      256 x 256 x 64 stack, 2-D radial nodes (256 spokes x 512 samples),
+      against 64 single 2-D plans;
+      3-D NFCT and NFST plans, N = 64^3, 2^20 nodes in [0, 1/2)^3 (fwd +
+      transpose, error vs the direct GPU sums on 64 nodes);
+      NFFTTools' sdc (20 iterations) on the 2-D spiral (config 5's nodes)."""
+    import torch
+    import nfftgb300 as nf
+    from nfftgb300 import tools
+    dev = torch.device("cuda", torch.cuda.current_device())
+    stream = torch.cuda.current_stream(dev)
+
+    def timed(fn):
+        for _ in range(args.warmup):
+            fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.steps):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) * 1e-3 / args.steps
+
+    def emit(metric, value, unit, ms, config, **extra):
+        line = {"metric": metric, "value": value, "unit": unit, "n_gpus": 1, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "data": "synthetic",
+                "config": config}
+        line.update(extra)
+        print(json.dumps(line), flush=True)
+
+    # ---- windows x precompute modes, 256^3 radial, FP32
+    k = radial_nodes(np.float32)
+    M = k.shape[1]
+    rng = np.random.default_rng(123)
+    f_h = complex_normal(rng, N3, np.complex128)
+    fh_h = complex_normal(rng, M, np.complex128)
+    f = nf.as_colmajor(f_h, N3, torch.complex64, dev)
+    fh = torch.as_tensor(fh_h).to(device=dev, dtype=torch.complex64)
+    y = torch.empty(M, dtype=torch.complex64, device=dev)
+    x = nf.empty_image(N3, torch.complex64, dev)
+    k64 = k.astype(np.float64)
+    rs = np.random.default_rng(7)
+    sub = rs.choice(M, 32, replace=False)
+    lin = rs.choice(int(np.prod(N3)), 16, replace=False)
+    ref_f = ndft_forward_subset(k64, f_h, sub)
+    ref_a = ndft_adjoint_subset(k64, N3, fh_h, lin)
+    table = {}
+    for window in ("kaiser_bessel", "gauss", "spline", "kaiser_bessel_rev", "cosh_type"):
+        for pre in ("TENSOR", "POLYNOMIAL", "LINEAR", "FULL"):
+            p = nf.plan_nfft(k, N3, m=4, sigma=2.0, window=window, precompute=getattr(nf, pre), blockSize=(16, 8, 8))
+            t = timed(lambda: (p.forward_(y, f), p.adjoint_(x, fh)))
+            yo = y.cpu().numpy()
+            xo = x.cpu().numpy().ravel(order="F")
+            table[f"{window}/{pre}"] = {"nodes_per_s": M / t, "ms": t * 1e3,
+                                        "err_fwd": rel_l2(yo[sub], ref_f), "err_adj": rel_l2(xo[lin], ref_a)}
+            del p
+            torch.cuda.empty_cache()
+    base = table["kaiser_bessel/TENSOR"]
+    emit("windows x precompute: fwd+adj NFFT nodes/s @256^3 radial FP32 m=4 (kaiser_bessel/TENSOR as value)",
+         base["nodes_per_s"], UNIT, base["ms"],
+         {"workload": WORKLOAD, "block_size": [16, 8, 8], "grid": "each plan's own"}, dtype="f32", table=table)
+    del f, fh, y, x
+    torch.cuda.empty_cache()
+
+    # ---- directional: 2-D NFFTs of the slices of a 256 x 256 x 64 stack
+    nsp, nsa = 256, 512
+    ang = np.arange(nsp) * np.pi * (3.0 - math.sqrt(5.0))
+    r = -0.5 + np.arange(nsa) / nsa
+    k2 = np.stack([np.outer(np.cos(ang), r).ravel(), np.outer(np.sin(ang), r).ravel()]).astype(np.float32)
+    J = k2.shape[1]
+    Nd = (256, 256, 64)
+    pd = nf.plan_nfft(k2, Nd, dims=(1, 2), m=4, sigma=2.0)
+    fd = nf.as_colmajor(complex_normal(rng, Nd), Nd, torch.complex64, dev)
+    vd = nf.as_colmajor(complex_normal(rng, pd.NOut), pd.NOut, torch.complex64, dev)
+    yd = nf.empty_image(pd.NOut, torch.complex64, dev)
+    xd = nf.empty_image(Nd, torch.complex64, dev)
+    t_dir = timed(lambda: (pd.forward_(yd, fd), pd.adjoint_(xd, vd)))
+    yd_h = yd.cpu().numpy()
+    ps = nf.plan_nfft(k2, (256, 256), m=4, sigma=2.0, precompute=nf.TENSOR)
+    ys = torch.empty(J, dtype=torch.complex64, device=dev)
+    xs = nf.empty_image((256, 256), torch.complex64, dev)
+    fsl = [fd[:, :, z].clone() for z in range(Nd[2])]
+    vsl = [vd[:, z].contiguous() for z in range(Nd[2])]
+
+    def loop():
+        for z in range(Nd[2]):
+            ps.forward_(ys, fsl[z])
+            ps.adjoint_(xs, vsl[z])
+    t_loop = timed(loop)
+    ps.forward_(ys, fsl[5])
+    d5 = rel_l2(yd_h[:, 5], ys.cpu().numpy())
+    emit("directional 2-D NFFT (dims 1:2) of a 256x256x64 stack: fwd+adj node values/s", J * Nd[2] / t_dir,
+         "node values/s", t_dir * 1e3,
+         {"workload": "N=(256,256,64), dims=1:2, 2-D golden-angle radial 256 spokes x 512 samples (J=131072), "
+                      "KB m=4 sigma=2, LINEAR (as the reference's directional plan)"},
+         dtype="f32", loop_of_64_single_2d_plans={"ms_per_step": t_loop * 1e3, "speedup_of_value": t_loop / t_dir},
+         rel_diff_slice5_vs_single_plan=d5)
+    del pd, ps, fd, vd, yd, xd, fsl, vsl
+    torch.cuda.empty_cache()
+
+    # ---- 3-D NFCT / NFST
+    Nt = (64, 64, 64)
+    Mt = 1 << 20
+    kt = (0.5 * rng.random((3, Mt))).astype(np.float32)
+    sel = rng.choice(Mt, 64, replace=False)
+    for kind in ("nfct", "nfst"):
+        plan = (nf.plan_nfct if kind == "nfct" else nf.plan_nfst)(kt, Nt, m=4, sigma=2.0)
+        shp = plan.size_in()
+        ft = nf.as_colmajor(rng.standard_normal(shp).astype(np.float32), shp, torch.float32, dev)
+        vt = torch.as_tensor(rng.standard_normal(Mt).astype(np.float32)).to(dev)
+        gt = torch.empty(Mt, dtype=torch.float32, device=dev)
+        xt = nf.empty_image(shp, torch.float32, dev)
+        t_t = timed(lambda: (plan.forward_(gt, ft), plan.transpose_(xt, vt)))
+        plan.forward_(gt, ft)
+        direct = (nf.NDCTPlan if kind == "nfct" else nf.NDSTPlan)(kt[:, sel], Nt) * ft
+        err = rel_l2(gt.cpu().numpy()[sel], direct.cpu().numpy())
+        emit(f"3-D {kind.upper()} fwd+transpose nodes/s, N=64^3, 2^20 nodes, FP32", Mt / t_t, UNIT, t_t * 1e3,
+             {"workload": f"{kind.upper()} N=64^3 (NFFT of 128^3), M=2^20 nodes in [0,1/2)^3, KB m=4 sigma=2"},
+             dtype="f32", rel_err_vs_direct_gpu_sums=err)
+        del plan, ft, vt, gt, xt
+        torch.cuda.empty_cache()
+
+    # ---- sdc on the 2-D spiral
+    ksp = spiral_nodes(256).astype(np.float32)
+    psd = nf.plan_nfft(ksp, (256, 256), m=4, sigma=2.0, precompute=nf.TENSOR)
+    t_sdc = timed(lambda: tools.sdc(psd, iters=20))
+    emit("NFFTTools sdc (20 iterations) on the 2-D spiral 256^2, FP32: weight sets/s", 1.0 / t_sdc, "weight sets/s",
+         t_sdc * 1e3, {"workload": "32 interleaves x 2048 samples, N=256^2, KB m=4 sigma=2, TENSOR"}, dtype="f32")
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -899,13 +1036,15 @@ def main():
                          "density; 134 MB grid, above L2) -- not a bench line")
     ap.add_argument("--workload", default="radial3d",
                     choices=["radial3d", "batched2d", "plain2d", "line1d", "spiral2d", "radial3d_fp64",
-                             "toeplitz3d"],
+                             "toeplitz3d", "extras"],
                     help="radial3d: the headline line; the others print extra lines for the other configurations")
     args = ap.parse_args()
     if args.workload == "batched2d":
         return run_batched(args)
     if args.workload == "toeplitz3d":
         return run_toeplitz(args)
+    if args.workload == "extras":
+        return run_extras(args)
     if args.workload in CONFIGS:
         return run_config(args)
     if args.small:

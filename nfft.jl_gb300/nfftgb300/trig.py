@@ -103,7 +103,9 @@ class _DirectPlan:
         return v
 
     def _cplx_of(self, t):
-        return self.complex_data or (isinstance(t, torch.Tensor) and t.is_complex()) or np.iscomplexobj(t)
+        if self.complex_data:
+            return True
+        return t.is_complex() if isinstance(t, torch.Tensor) else bool(np.iscomplexobj(t))
 
     def forward_(self, fHat, f):
         """mul!(fHat, p, f)."""
