@@ -53,15 +53,24 @@ __device__ __forceinline__ void interp_node(const Geom<T>& G, const Nodes<T>& Nd
 #pragma unroll
       for (int s = 0; s < LN::NSTEP; ++s) v[iz][s] = __ldg(gp + row[s]);
     }
+    // sum over z first, then weight by wx wy: 2.4 instead of 3 multiply-adds
+    // per tap (what bounds the FP64 gather on GB300's FP64 units)
+    T sr[LN::NSTEP], si[LN::NSTEP];
+#pragma unroll
+    for (int s = 0; s < LN::NSTEP; ++s) sr[s] = si[s] = T(0);
 #pragma unroll
     for (int iz = 0; iz < L; ++iz) {
       const T wz = wsel<D, L>(W, 2 * L + iz);
 #pragma unroll
       for (int s = 0; s < LN::NSTEP; ++s) {
-        const T w = wxy[s] * wz;
-        ar = fma(w, v[iz][s].x, ar);
-        ai = fma(w, v[iz][s].y, ai);
+        sr[s] = fma(wz, v[iz][s].x, sr[s]);
+        si[s] = fma(wz, v[iz][s].y, si[s]);
       }
+    }
+#pragma unroll
+    for (int s = 0; s < LN::NSTEP; ++s) {
+      ar = fma(wxy[s], sr[s], ar);
+      ai = fma(wxy[s], si[s], ai);
     }
   }
 #pragma unroll
