@@ -19,6 +19,7 @@ shard); value is the aggregate over ranks.
 from __future__ import annotations
 
 import argparse
+import atexit
 import json
 import math
 import os
@@ -78,33 +79,47 @@ def measured_peak_hbm():
 
 
 class ClockSampler:
-    """nvidia-smi clock/throttle samples during the timed region."""
+    """nvidia-smi clock/throttle samples (every 50 ms, with nvidia-smi's own
+    timestamps).  Start it well before the timed region (nvidia-smi takes a
+    moment to come up), bracket the timed region with mark_start() /
+    mark_end(), and summary() keeps the samples taken inside it."""
 
-    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+    FIELDS = ("timestamp,index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
-    def __init__(self, gpu_index=0):
+    def __init__(self, gpu_index=0, interval_ms=50):
         self.proc = None
         self.gpu_index = gpu_index
+        self.interval_ms = interval_ms
         self.out = []
+        self.t0 = self.t1 = None
 
-    def __enter__(self):
+    def start(self):
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", f"--id={self.gpu_index}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
-                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+                 "-lms", str(self.interval_ms)], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self._t = threading.Thread(target=self._read, daemon=True)
             self._t.start()
         except Exception:
             self.proc = None
         return self
 
+    def __enter__(self):
+        return self.start()
+
+    def mark_start(self):
+        self.t0 = time.time()
+
+    def mark_end(self):
+        self.t1 = time.time()
+
     def _read(self):
         for line in self.proc.stdout:
             self.out.append(line.strip())
 
-    def __exit__(self, *a):
+    def stop(self):
         if self.proc is not None:
             self.proc.terminate()
             try:
@@ -112,28 +127,41 @@ class ClockSampler:
             except Exception:
                 self.proc.kill()
             self._t.join(timeout=2)
+            self.proc = None
+
+    def __exit__(self, *a):
+        self.stop()
 
     def summary(self):
-        if not self.out:
-            return None
-        sm, mx, reasons = [], None, set()
-        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        import datetime
+        rows = []
         for line in self.out:
             parts = [p.strip() for p in line.split(",")]
-            if len(parts) < 9:
+            if len(parts) < 10:
                 continue
             try:
-                sm.append(float(parts[1]))
-                mx = float(parts[2])
+                ts = datetime.datetime.strptime(parts[0], "%Y/%m/%d %H:%M:%S.%f").timestamp()
+                rows.append((ts, float(parts[2]), float(parts[3]), parts[6:10]))
             except ValueError:
                 continue
-            for nm, val in zip(names, parts[5:9]):
+        if not rows:
+            return None
+        window = "timed region"
+        if self.t0 is not None and self.t1 is not None:
+            inside = [r for r in rows if self.t0 - 0.005 <= r[0] <= self.t1 + 0.005]
+            if not inside:  # region shorter than the interval: the sample nearest to its middle
+                mid = 0.5 * (self.t0 + self.t1)
+                inside = [min(rows, key=lambda r: abs(r[0] - mid))]
+                window = "nearest sample to the timed region"
+            rows = inside
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        for r in rows:
+            for nm, val in zip(names, r[3]):
                 if val.lower().startswith("active"):
                     reasons.add(nm)
-        if not sm:
-            return None
-        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons),
-                "samples": len(sm)}
+        return {"sm_mhz": statistics.median(r[1] for r in rows), "sm_max_mhz": rows[-1][2],
+                "reasons": sorted(reasons), "samples": len(rows), "window": window}
 
 
 def ndft_forward_subset(k64, f, sub):
@@ -264,6 +292,8 @@ def run_ours(args):
         dist.init_process_group("nccl")
     dev = torch.device("cuda", torch.cuda.current_device())
 
+    clk = ClockSampler(local).start()  # up and sampling before the timed region
+    atexit.register(clk.stop)          # never leave nvidia-smi running
     k = radial_nodes(np.float32)
     rng = np.random.default_rng(123)
     f_h = complex_normal(rng, N3)
@@ -296,17 +326,19 @@ def run_ours(args):
     launches0 = nf.kernel_launch_count()
     stream = torch.cuda.current_stream(dev)
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    with ClockSampler(local) as clk:
-        if world > 1:
-            dist.barrier()
-        torch.cuda.synchronize()
-        ev0.record(stream)
-        for _ in range(args.steps):
-            step()
-        ev1.record(stream)
-        torch.cuda.synchronize()
-        if world > 1:
-            dist.barrier()
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    clk.mark_start()
+    ev0.record(stream)
+    for _ in range(args.steps):
+        step()
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    clk.mark_end()
+    if world > 1:
+        dist.barrier()
+    clk.stop()
     launches = nf.kernel_launch_count() - launches0
     t_dev = max_over_ranks(ev0.elapsed_time(ev1) * 1e-3, world, dev)
     value = aggregate_nodes_per_s(world, M_NODES, args.steps, t_dev)
@@ -819,7 +851,13 @@ def run_toeplitz(args):
         return e0.elapsed_time(e1) * 1e-3 / args.steps, (nf.kernel_launch_count() - l0) // args.steps
 
     with ClockSampler(torch.cuda.current_device()) as clk:
+        time.sleep(0.3)  # nvidia-smi up and sampling before the timed region
+        for _ in range(args.warmup):
+            tz.convolve_(y, lam_t)
+        torch.cuda.synchronize()
+        clk.mark_start()
         t_fused, launches = timed(lambda: tz.convolve_(y, lam_t))
+        clk.mark_end()
     t_cufft, _ = timed(lambda: ref.convolve_(y2, lam_t))
     t_pair, _ = timed(lambda: (p.forward_(fh, x), p.adjoint_(xa, fh)))
     # one application of the true kernel against A^H A through the NFFT pair
@@ -1021,7 +1059,7 @@ def run_extras(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=40)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--precompute", default="tensor", choices=["tensor", "polynomial", "full", "linear"],

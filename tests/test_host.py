@@ -66,3 +66,31 @@ def test_bench_ndft_checker_matches_oracle():
     sub, lin = np.arange(0, M, 3), np.arange(0, 480, 7)
     assert oracle.rel_l2(bench.ndft_forward_subset(k, f, sub), oracle.ndft_forward(k, f, subset=sub)) < 1e-13
     assert oracle.rel_l2(bench.ndft_adjoint_subset(k, N, fh, lin), oracle.ndft_adjoint(k, N, fh, subset=lin)) < 1e-13
+
+
+def test_bench_clock_sampler_keeps_the_timed_region():
+    """bench.py's clock record: nvidia-smi lines (timestamp first) are parsed,
+    only samples inside the marked timed region count, throttle reasons are
+    collected, and a region shorter than the interval takes the nearest
+    sample."""
+    import datetime
+    import bench
+    t0 = datetime.datetime(2026, 1, 2, 3, 4, 5, 0)
+
+    def line(dt_ms, sm, reasons=("Not Active",) * 4):
+        ts = (t0 + datetime.timedelta(milliseconds=dt_ms)).strftime("%Y/%m/%d %H:%M:%S.%f")[:-3]
+        return ", ".join([ts, "0", str(sm), "2070", "800.00 W", "0x0"] + list(reasons))
+
+    cs = bench.ClockSampler()
+    cs.out = [line(0, 1000), line(50, 2070), line(100, 2060, ("Not Active", "Not Active", "Not Active", "Active")),
+              line(150, 2070), line(200, 900)]
+    base = t0.timestamp()
+    cs.t0, cs.t1 = base + 0.040, base + 0.160
+    s = cs.summary()
+    assert s["samples"] == 3 and s["sm_mhz"] == 2070 and s["sm_max_mhz"] == 2070
+    assert s["reasons"] == ["sw_power_cap"] and s["window"] == "timed region"
+    cs.t0, cs.t1 = base + 0.060, base + 0.070
+    s = cs.summary()
+    assert s["samples"] == 1 and s["sm_mhz"] == 2070 and s["window"].startswith("nearest")
+    cs.out = ["garbage", ""]
+    assert cs.summary() is None
