@@ -47,6 +47,10 @@ WORKLOAD = "3D radial koosh-ball NFFT fwd+adj, N=256^3, 8192 spokes x 512 sample
 # (profiles/spread_owned_radial256.md: 1.115 GB read + 0.564 GB write).
 SPREAD_DRAM_BYTES = 1.679e9
 # What bounds the dominant kernel on chip (same capture).
+# DRAM bytes (read + write) of one Toeplitz application at 256^3 (the five
+# kernels of the fused path), from the ncu launch list of the profiling case
+# (profiles/toeplitz_apply_256.md: 2.821 GB read + 1.049 GB write).
+TOEPLITZ_DRAM_BYTES = 3.870e9
 SPREAD_LIMITER = ("shared-memory pipe 73.3% and instruction issue 81.6% of peak (ncu); the 20 B of shared-memory "
                   "traffic per tap put the tap phase at 1.07 ms, HBM is not the limiter")
 
@@ -891,7 +895,7 @@ def run_toeplitz(args):
                                                 "fft4_lines_kernel, fft4_x_kernel (whole application)",
                      "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "peak_source": peak_src, "algorithmic_bytes": design_bytes,
-                     "compulsory_bytes": compulsory, "traffic": None},
+                     "compulsory_bytes": compulsory, "traffic": TOEPLITZ_DRAM_BYTES},
         "cufft_sequence": {"ms_per_step": t_cufft * 1e3, "speedup_of_value": t_cufft / t_fused,
                            "rel_diff_vs_fused": d_cufft,
                            "what": "the reference's sequence on the GPU: zero-fill + corner copy, cuFFT, "
