@@ -215,7 +215,7 @@ extern "C" int nfft_direct(int kind, int precision, int D, const int64_t* N, int
     set_error("D = %d not supported by the direct transforms (1..%d)", D, kDirMaxD);
     return NFFT_ERR_INVALID_ARG;
   }
-  if (!N || M < 0 || (M > 0 && !k) || !in || !out) {
+  if (!N || M < 0 || (M > 0 && !k)) {
     set_error("null argument or negative node count");
     return NFFT_ERR_INVALID_ARG;
   }
@@ -247,6 +247,13 @@ extern "C" int nfft_direct(int kind, int precision, int D, const int64_t* N, int
       G.ext[d] = e;
       G.off[d] = kind == NFFT_NDFT ? -(n / 2) : (kind == NFFT_NDST ? 1 : 0);
       G.n_img *= e;
+    }
+  }
+  {
+    const int64_t n_in = adjoint ? M : G.n_img, n_out = adjoint ? G.n_img : M;
+    if ((n_in > 0 && !in) || (n_out > 0 && !out)) {
+      set_error("null data pointer");
+      return NFFT_ERR_INVALID_ARG;
     }
   }
   if (M == 0 || G.n_img == 0) {

@@ -180,3 +180,12 @@ def test_gram_large_3d_fused_vs_cufft():
     lhs = torch.vdot(x.flatten().to(torch.complex128), ty.flatten().to(torch.complex128))
     rhs = torch.vdot(tx.flatten().to(torch.complex128), yv.flatten().to(torch.complex128))
     assert abs(complex(lhs - rhs)) < 1e-4 * abs(complex(lhs))
+
+
+def test_toeplitz_kernel_of_empty_node_set_is_zero():
+    tz = tools.Toeplitz((32, 32), torch.complex64)
+    lam = tools.calculate_toeplitz_kernel((32, 32), np.zeros((2, 0), np.float32), toeplitz=tz)
+    assert float(lam.abs().max()) == 0.0
+    y = nf.as_colmajor(np.ones((32, 32), np.complex64), (32, 32), torch.complex64)
+    tz.convolve_(y, lam)
+    assert float(y.abs().max()) == 0.0

@@ -167,3 +167,31 @@ def test_trig_nodes_and_errors():
         nf.NDFTPlan(k1, (8,))
     with pytest.raises(nf.ArgumentError):
         nf.plan_nfst(k1 + 1.0, N)                # nodes beyond 1/2
+
+
+def test_empty_node_sets():
+    """M = 0: forward outputs are empty, transposes / adjoints are zero images."""
+    N = (8, 6)
+    k0 = np.zeros((2, 0))
+    p = nf.NDFTPlan(k0, N)
+    assert host(p.adjoint() * np.zeros(0, complex)).shape == N
+    assert np.all(host(p.adjoint() * np.zeros(0, complex)) == 0)
+    assert host(p * np.ones(N, complex)).shape == (0,)
+    c = nf.plan_nfct(k0, N)
+    assert np.all(host(c.transpose() * np.zeros(0)) == 0)
+    assert host(c * np.ones(N)).shape == (0,)
+    s = nf.plan_nfst(k0, (8, 7))
+    assert np.all(host(s.transpose() * np.zeros(0)) == 0)
+
+
+def test_ndst_with_single_point_dimension():
+    """N_d = 2 gives a single sine term n_d = 1 in that dimension."""
+    rng = np.random.default_rng(8)
+    k = 0.5 * rng.random((2, 50))
+    N = (2, 9)
+    f = rng.standard_normal((1, 8))
+    p = nf.NDSTPlan(k, N)
+    assert p.size_in() == (1, 8)
+    assert rel(host(p * f), oracle.ndst_forward(k, f)) < 1e-12
+    q = nf.plan_nfst(k, N, m=5, sigma=2.0)
+    assert rel(host(q * f), oracle.ndst_forward(k, f)) < 1e-7
