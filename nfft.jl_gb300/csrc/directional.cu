@@ -39,6 +39,11 @@ struct nfft_dplan {
   bool fft_loop = false;           // one exec per post column block
   void* fft_work = nullptr;
   bool has_nodes = false;
+  // pre == 1 (the transform dims lead): every column is an ordinary image of
+  // the transform dims, so the core plan bins the nodes once and its tiled
+  // gather / atomic-free spreader run column by column
+  bool tiled = false;
+  void* sorted = nullptr;          // tiled: bin-sorted node values of every column (M x post complex)
 };
 
 namespace nfft {
@@ -303,14 +308,31 @@ template <typename T> int dforward(nfft_dplan* q, const void* f, void* fhat) {
   NFFT_LAUNCH_CHECK();
   int rc = dexec_fft(q, CUFFT_FORWARD);
   if (rc) return rc;
+  if (q->tiled) {  // all columns in one launch (at most 65535 per launch)
+    for (int64_t c0 = 0; c0 < q->post && !rc; c0 += 65535) {
+      const int nc = int(q->post - c0 < 65535 ? q->post - c0 : 65535);
+      rc = launch_interp_cols(q->core, static_cast<const C*>(q->grid) + c0 * q->Rnt,
+                              static_cast<C*>(fhat) + c0 * q->M, nc, q->Rnt, q->M);
+    }
+    return rc;
+  }
   return dconv<T>(q, q->grid, fhat, false);
 }
 
 template <typename T> int dadjoint(nfft_dplan* q, const void* fhat, void* f) {
   using C = typename Cplx<T>::type;
   DGeom<T> G = make_dgeom<T>(q);
-  NFFT_CUDA_TRY(cudaMemsetAsync(q->grid, 0, 2 * sizeof(T) * size_t(q->pre * q->Rnt * q->post), q->stream));
-  int rc = dconv<T>(q, fhat, q->grid, true);
+  int rc = NFFT_OK;
+  if (q->tiled) {  // the spreader zeroes the column grids itself
+    for (int64_t c0 = 0; c0 < q->post && !rc; c0 += 65535) {
+      const int nc = int(q->post - c0 < 65535 ? q->post - c0 : 65535);
+      rc = launch_spread_cols(q->core, static_cast<const C*>(fhat) + c0 * q->M, static_cast<C*>(q->grid) + c0 * q->Rnt,
+                              nc, q->M, q->Rnt, q->sorted);
+    }
+  } else {
+    NFFT_CUDA_TRY(cudaMemsetAsync(q->grid, 0, 2 * sizeof(T) * size_t(q->pre * q->Rnt * q->post), q->stream));
+    rc = dconv<T>(q, fhat, q->grid, true);
+  }
   if (rc) return rc;
   rc = dexec_fft(q, CUFFT_INVERSE);
   if (rc) return rc;
@@ -331,6 +353,7 @@ extern "C" int nfft_dplan_destroy(nfft_dplan* q) {
   cudaFree(q->fft_work);
   cudaFree(q->grid);
   cudaFree(q->k);
+  cudaFree(q->sorted);
   if (q->core) nfft_plan_destroy(q->core);
   delete q;
   return NFFT_OK;
@@ -367,7 +390,8 @@ extern "C" int nfft_dplan_create(nfft_dplan** out, int precision, int D, const i
   // the core plan: the transform dims, LINEAR window (src/implementation.jl:80-82)
   nfft_params prm = *params;
   prm.precompute = NFFT_PRECOMPUTE_LINEAR;
-  prm.blocking = 0;
+  q->tiled = dim_lo == 0 && M > 0;
+  prm.blocking = q->tiled ? 1 : 0;
   prm.compensated = 0;
   prm.timing = 0;
   int64_t Nc[3] = {1, 1, 1};
@@ -390,6 +414,14 @@ extern "C" int nfft_dplan_create(nfft_dplan** out, int precision, int D, const i
     nfft_dplan_destroy(q);
     set_error("cudaMalloc of the directional grid failed");
     return NFFT_ERR_ALLOC;
+  }
+  if (q->tiled) {
+    const int64_t per = q->post < 65535 ? q->post : 65535;
+    if (cudaMalloc(&q->sorted, 2 * rs * size_t(M) * size_t(per)) != cudaSuccess) {
+      nfft_dplan_destroy(q);
+      set_error("cudaMalloc of the sorted node values failed");
+      return NFFT_ERR_ALLOC;
+    }
   }
   // cuFFT along the transform dims (C order: reversed), columns batched
   int n[3];
@@ -436,8 +468,9 @@ extern "C" int nfft_dplan_set_nodes(nfft_dplan* q, const void* k, int k_on_devic
   if (bytes)
     NFFT_CUDA_TRY(cudaMemcpyAsync(q->k, k, bytes, k_on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
                                   q->stream));
-  const int rc = q->precision == 32 ? dcheck_nodes<float>(q) : dcheck_nodes<double>(q);
+  int rc = q->precision == 32 ? dcheck_nodes<float>(q) : dcheck_nodes<double>(q);
   if (rc) return rc;
+  if (q->tiled && (rc = nfft_set_nodes(q->core, q->k, 1))) return rc;
   q->has_nodes = true;
   return NFFT_OK;
 }

@@ -26,12 +26,17 @@ template <typename C> __device__ __forceinline__ void cp_async_elem(C* smem, con
 }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
 
-template <int D, int L, typename T, bool TABLE>
+template <int D, int L, typename T, bool TABLE, bool COLS = false>
 __global__ void __launch_bounds__(kInterpThreads) interp_kernel(Geom<T> G, Nodes<T> Nd,
                                                                  const typename Cplx<T>::type* __restrict__ g,
-                                                                 typename Cplx<T>::type* __restrict__ fhat) {
+                                                                 typename Cplx<T>::type* __restrict__ fhat,
+                                                                 int64_t gcol = 0, int64_t fcol = 0) {
   using C = typename Cplx<T>::type;
   using LN = Lanes<D, L>;
+  if constexpr (COLS) {  // column of a multi-column launch
+    g += blockIdx.y * gcol;
+    fhat += blockIdx.y * fcol;
+  }
   const int lane = threadIdx.x & 31;
   const int64_t warp_global = int64_t(blockIdx.x) * (blockDim.x >> 5) + (threadIdx.x >> 5);
   const int64_t warps_total = int64_t(gridDim.x) * (blockDim.x >> 5);
@@ -242,18 +247,28 @@ __global__ void __launch_bounds__(kInterpThreads) interp_tile_kernel(Geom<T> G, 
   }
 }
 
+// ncols columns in one launch (blockIdx.y): grids g + c gcol, values fhat + c fcol.
 template <int D, int L, typename T>
-int interp_launch(const nfft_plan* p, const void* g, void* fhat) {
+int interp_launch(const nfft_plan* p, const void* g, void* fhat, int ncols, int64_t gcol, int64_t fcol) {
   Geom<T> G = make_geom<T>(p);
   Nodes<T> Nd = make_nodes<T>(p);
   if (Nd.M == 0) return NFFT_OK;
   using C = typename Cplx<T>::type;
   const int64_t per_block = (kInterpThreads / 32) * (D == 1 ? Lanes<D, L>::NPW : 1);
   int64_t blocks = (Nd.M + per_block - 1) / per_block;
-  const int64_t cap = 152 * 64;
+  const int64_t cap = (152 * 64 + ncols - 1) / ncols;
   if (blocks > cap) blocks = cap;
   const C* gp = static_cast<const C*>(g);
   C* fp = static_cast<C*>(fhat);
+  if (ncols > 1) {
+    const dim3 grid{unsigned(blocks), unsigned(ncols), 1u};
+    if (p->wtab)
+      interp_kernel<D, L, T, true, true><<<grid, kInterpThreads, 0, p->stream>>>(G, Nd, gp, fp, gcol, fcol);
+    else
+      interp_kernel<D, L, T, false, true><<<grid, kInterpThreads, 0, p->stream>>>(G, Nd, gp, fp, gcol, fcol);
+    NFFT_LAUNCH_CHECK();
+    return NFFT_OK;
+  }
   if (p->tasks && p->gather_tiled) {
     const int P1 = D >= 2 ? int(p->bs[1]) + L - 1 : 1;
     const int P2 = D == 3 ? int(p->bs[2]) + L - 1 : 1;
@@ -274,33 +289,42 @@ int interp_launch(const nfft_plan* p, const void* g, void* fhat) {
   return NFFT_OK;
 }
 
-template <int D, typename T> int interp_dispatch_l(const nfft_plan* p, const void* g, void* fhat) {
+#define NFFT_INTERP_ARGS p, g, fhat, ncols, gcol, fcol
+template <int D, typename T>
+int interp_dispatch_l(const nfft_plan* p, const void* g, void* fhat, int ncols, int64_t gcol, int64_t fcol) {
   switch (p->m) {
-    case 2: return interp_launch<D, 4, T>(p, g, fhat);
-    case 3: return interp_launch<D, 6, T>(p, g, fhat);
-    case 4: return interp_launch<D, 8, T>(p, g, fhat);
-    case 5: return interp_launch<D, 10, T>(p, g, fhat);
-    case 6: return interp_launch<D, 12, T>(p, g, fhat);
-    case 7: return interp_launch<D, 14, T>(p, g, fhat);
-    case 8: return interp_launch<D, 16, T>(p, g, fhat);
+    case 2: return interp_launch<D, 4, T>(NFFT_INTERP_ARGS);
+    case 3: return interp_launch<D, 6, T>(NFFT_INTERP_ARGS);
+    case 4: return interp_launch<D, 8, T>(NFFT_INTERP_ARGS);
+    case 5: return interp_launch<D, 10, T>(NFFT_INTERP_ARGS);
+    case 6: return interp_launch<D, 12, T>(NFFT_INTERP_ARGS);
+    case 7: return interp_launch<D, 14, T>(NFFT_INTERP_ARGS);
+    case 8: return interp_launch<D, 16, T>(NFFT_INTERP_ARGS);
   }
   set_error("m = %d not supported (2..8)", p->m);
   return NFFT_ERR_UNSUPPORTED;
 }
 
-template <typename T> int interp_dispatch(const nfft_plan* p, const void* g, void* fhat) {
+template <typename T>
+int interp_dispatch(const nfft_plan* p, const void* g, void* fhat, int ncols, int64_t gcol, int64_t fcol) {
   switch (p->D) {
-    case 1: return interp_dispatch_l<1, T>(p, g, fhat);
-    case 2: return interp_dispatch_l<2, T>(p, g, fhat);
-    case 3: return interp_dispatch_l<3, T>(p, g, fhat);
+    case 1: return interp_dispatch_l<1, T>(NFFT_INTERP_ARGS);
+    case 2: return interp_dispatch_l<2, T>(NFFT_INTERP_ARGS);
+    case 3: return interp_dispatch_l<3, T>(NFFT_INTERP_ARGS);
   }
   return NFFT_ERR_UNSUPPORTED;
 }
+#undef NFFT_INTERP_ARGS
 
 }  // namespace
 
 int launch_interp(const nfft_plan* p, const void* g, int, void* fhat, int) {
-  return p->precision == 32 ? interp_dispatch<float>(p, g, fhat) : interp_dispatch<double>(p, g, fhat);
+  return p->precision == 32 ? interp_dispatch<float>(p, g, fhat, 1, 0, 0) : interp_dispatch<double>(p, g, fhat, 1, 0, 0);
+}
+
+int launch_interp_cols(const nfft_plan* p, const void* g, void* fhat, int ncols, int64_t gcol, int64_t fcol) {
+  return p->precision == 32 ? interp_dispatch<float>(p, g, fhat, ncols, gcol, fcol)
+                            : interp_dispatch<double>(p, g, fhat, ncols, gcol, fcol);
 }
 
 }  // namespace nfft

@@ -179,8 +179,13 @@ int launch_real_to_complex(const nfft_plan* p, const void* in, void* out, int64_
 int launch_real_part(const nfft_plan* p, const void* in, void* out, int64_t n);
 // interp.cu
 int launch_interp(const nfft_plan* p, const void* g, int g_real, void* fhat, int fhat_real);
+// ncols columns in one launch: grids g + c gcol, node values fhat + c fcol (complex elements)
+int launch_interp_cols(const nfft_plan* p, const void* g, void* fhat, int ncols, int64_t gcol, int64_t fcol);
 // spread.cu
 int launch_spread(nfft_plan* p, const void* fhat, int fhat_real, void* g, int g_real);
+// ncols columns in one launch: values fhat + c fcol, contiguous grids g + c gcol (gcol = |Ntilde|),
+// bin-sorted values in `sorted` (M x ncols complex)
+int launch_spread_cols(nfft_plan* p, const void* fhat, void* g, int ncols, int64_t fcol, int64_t gcol, void* sorted);
 // plan.cu: the grid FFT of a plan (pruned for D >= 2)
 int exec_fft_plan(nfft_plan* p, int dir);
 // fft.cu: fused pruned FFT with the deconvolution

@@ -27,23 +27,34 @@ namespace nfft {
 namespace {
 
 // fHat in bin-sorted order (node4[i].w = input index), for coalesced staging.
+// blockIdx.y: column of a multi-column launch (input fhat + y fcol, output out + y M)
 template <typename T>
 __global__ void sort_values_kernel(const int4* __restrict__ node4, const typename Cplx<T>::type* __restrict__ fhat,
-                                   typename Cplx<T>::type* __restrict__ out, int64_t M) {
+                                   typename Cplx<T>::type* __restrict__ out, int64_t M, int64_t fcol = 0) {
+  fhat += blockIdx.y * fcol;
+  out += blockIdx.y * M;
   for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < M; i += int64_t(gridDim.x) * blockDim.x)
     out[i] = __ldg(fhat + __ldg(node4 + i).w);
 }
 
+// ncols columns in one launch (blockIdx.y): values fhat + c fcol, grids
+// g + c gcol (complex elements; the grids must be contiguous, gcol = |Ntilde|),
+// bin-sorted values in `sorted` (M x ncols); ncols = 1 uses the plan's own scratch.
 template <int D, int L, typename T>
-int spread_launch(nfft_plan* p, const void* fhat, void* g) {
+int spread_launch(nfft_plan* p, const void* fhat, void* g, int ncols, int64_t fcol, int64_t gcol, void* sorted) {
   Geom<T> G = make_geom<T>(p);
   Nodes<T> Nd = make_nodes<T>(p);
   using C = typename Cplx<T>::type;
   const size_t gbytes = size_t(p->Nt[0] * p->Nt[1] * p->Nt[2]) * sizeof(T) * 2;
-  NFFT_CUDA_TRY(cudaMemsetAsync(g, 0, gbytes, p->stream));
+  NFFT_CUDA_TRY(cudaMemsetAsync(g, 0, gbytes * size_t(ncols), p->stream));
   if (p->n_tasks == 0) return NFFT_OK;
   const C* fp = static_cast<const C*>(fhat);
   T* gp = static_cast<T*>(g);
+  const int64_t gcol_t = 2 * gcol;  // in T units
+  if (ncols > 1 && (p->prm.compensated || (D == 3 && p->spread_ny == 2))) {
+    set_error("multi-column spreading supports the default (uncompensated, 8-warp) tiles only");
+    return NFFT_ERR_UNSUPPORTED;
+  }
   if constexpr (D == 1) {
     if (p->prm.compensated) {
       const size_t smem = ((sizeof(typename Acc<T, true>::type) * size_t(p->bs[0] + L - 1) + 31) & ~size_t(31)) +
@@ -66,7 +77,8 @@ int spread_launch(nfft_plan* p, const void* fhat, void* g) {
     }
     auto kern = p->wtab ? spread_pad1_kernel<L, T, true> : spread_pad1_kernel<L, T, false>;
     NFFT_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
-    kern<<<unsigned(p->n_tasks), kSpreadThreads, smem, p->stream>>>(G, Nd, p->tasks, fp, gp);
+    kern<<<dim3(unsigned(p->n_tasks), unsigned(ncols)), kSpreadThreads, smem, p->stream>>>(G, Nd, p->tasks, fp, gp,
+                                                                                          fcol, gcol_t);
   } else {
     const bool comp = p->prm.compensated != 0;
     const size_t smem = owned_smem<D, L, T>(p, comp);
@@ -84,39 +96,45 @@ int spread_launch(nfft_plan* p, const void* fhat, void* g) {
       }
     }
     NFFT_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
-    C* fs = static_cast<C*>(p->fsorted);
+    C* fs = static_cast<C*>(ncols > 1 ? sorted : p->fsorted);
     int64_t nb = (p->M + 255) / 256;
-    if (nb > 152 * 32) nb = 152 * 32;
-    sort_values_kernel<T><<<unsigned(nb), 256, 0, p->stream>>>(p->node4, fp, fs, p->M);
+    const int64_t cap = (152 * 32 + ncols - 1) / ncols;
+    if (nb > cap) nb = cap;
+    sort_values_kernel<T><<<dim3(unsigned(nb), unsigned(ncols)), 256, 0, p->stream>>>(p->node4, fp, fs, p->M, fcol);
     NFFT_LAUNCH_CHECK();
-    kern<<<unsigned(p->n_tasks), threads, smem, p->stream>>>(G, Nd, p->tasks, fs, gp, p->spread_pitch);
+    kern<<<dim3(unsigned(p->n_tasks), unsigned(ncols)), threads, smem, p->stream>>>(G, Nd, p->tasks, fs, gp,
+                                                                                   p->spread_pitch, p->M, gcol_t);
   }
   NFFT_LAUNCH_CHECK();
   return NFFT_OK;
 }
 
-template <int D, typename T> int spread_dispatch_l(nfft_plan* p, const void* fhat, void* g) {
+#define NFFT_SPREAD_ARGS p, fhat, g, ncols, fcol, gcol, sorted
+template <int D, typename T>
+int spread_dispatch_l(nfft_plan* p, const void* fhat, void* g, int ncols, int64_t fcol, int64_t gcol, void* sorted) {
   switch (p->m) {
-    case 2: return spread_launch<D, 4, T>(p, fhat, g);
-    case 3: return spread_launch<D, 6, T>(p, fhat, g);
-    case 4: return spread_launch<D, 8, T>(p, fhat, g);
-    case 5: return spread_launch<D, 10, T>(p, fhat, g);
-    case 6: return spread_launch<D, 12, T>(p, fhat, g);
-    case 7: return spread_launch<D, 14, T>(p, fhat, g);
-    case 8: return spread_launch<D, 16, T>(p, fhat, g);
+    case 2: return spread_launch<D, 4, T>(NFFT_SPREAD_ARGS);
+    case 3: return spread_launch<D, 6, T>(NFFT_SPREAD_ARGS);
+    case 4: return spread_launch<D, 8, T>(NFFT_SPREAD_ARGS);
+    case 5: return spread_launch<D, 10, T>(NFFT_SPREAD_ARGS);
+    case 6: return spread_launch<D, 12, T>(NFFT_SPREAD_ARGS);
+    case 7: return spread_launch<D, 14, T>(NFFT_SPREAD_ARGS);
+    case 8: return spread_launch<D, 16, T>(NFFT_SPREAD_ARGS);
   }
   set_error("m = %d not supported (2..8)", p->m);
   return NFFT_ERR_UNSUPPORTED;
 }
 
-template <typename T> int spread_dispatch(nfft_plan* p, const void* fhat, void* g) {
+template <typename T>
+int spread_dispatch(nfft_plan* p, const void* fhat, void* g, int ncols, int64_t fcol, int64_t gcol, void* sorted) {
   switch (p->D) {
-    case 1: return spread_dispatch_l<1, T>(p, fhat, g);
-    case 2: return spread_dispatch_l<2, T>(p, fhat, g);
-    case 3: return spread_dispatch_l<3, T>(p, fhat, g);
+    case 1: return spread_dispatch_l<1, T>(NFFT_SPREAD_ARGS);
+    case 2: return spread_dispatch_l<2, T>(NFFT_SPREAD_ARGS);
+    case 3: return spread_dispatch_l<3, T>(NFFT_SPREAD_ARGS);
   }
   return NFFT_ERR_UNSUPPORTED;
 }
+#undef NFFT_SPREAD_ARGS
 
 }  // namespace
 
@@ -150,7 +168,14 @@ int spread_pitch_for(int D, int m, int P0, int elem_bytes, int ny) {
 }
 
 int launch_spread(nfft_plan* p, const void* fhat, int, void* g, int) {
-  return p->precision == 32 ? spread_dispatch<float>(p, fhat, g) : spread_dispatch<double>(p, fhat, g);
+  return p->precision == 32 ? spread_dispatch<float>(p, fhat, g, 1, 0, 0, nullptr)
+                            : spread_dispatch<double>(p, fhat, g, 1, 0, 0, nullptr);
+}
+
+int launch_spread_cols(nfft_plan* p, const void* fhat, void* g, int ncols, int64_t fcol, int64_t gcol,
+                       void* sorted) {
+  return p->precision == 32 ? spread_dispatch<float>(p, fhat, g, ncols, fcol, gcol, sorted)
+                            : spread_dispatch<double>(p, fhat, g, ncols, fcol, gcol, sorted);
 }
 
 }  // namespace nfft

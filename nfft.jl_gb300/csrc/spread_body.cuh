@@ -381,8 +381,11 @@ template <int D, int L, typename T, bool TABLE, bool KAHAN, int NY = 1>
 __global__ void __launch_bounds__(OwnedCfg<D, L, NY>::THREADS) spread_owned_kernel(Geom<T> G, Nodes<T> Nd,
                                                                                const int4* __restrict__ tasks,
                                                                                const typename Cplx<T>::type* __restrict__ fsorted,
-                                                                               T* __restrict__ g, int pitch) {
-  spread_owned_body<D, L, T, TABLE, KAHAN, NY>(G, Nd, tasks[blockIdx.x], fsorted, g, pitch);
+                                                                               T* __restrict__ g, int pitch,
+                                                                               int64_t fcol = 0, int64_t gcol = 0) {
+  // blockIdx.y: column of a multi-column launch (values fsorted + y fcol, grid g + y gcol)
+  spread_owned_body<D, L, T, TABLE, KAHAN, NY>(G, Nd, tasks[blockIdx.x], fsorted + blockIdx.y * fcol,
+                                               g + blockIdx.y * gcol, pitch);
 }
 
 // --------------------------------------------------------------------------
@@ -391,10 +394,13 @@ template <int L, typename T, bool TABLE>
 __global__ void __launch_bounds__(kSpreadThreads) spread_pad1_kernel(Geom<T> G, Nodes<T> Nd,
                                                                       const int4* __restrict__ tasks,
                                                                       const typename Cplx<T>::type* __restrict__ fhat,
-                                                                      T* __restrict__ g) {
+                                                                      T* __restrict__ g, int64_t fcol = 0,
+                                                                      int64_t gcol = 0) {
   using C = typename Cplx<T>::type;
   using LN = Lanes<1, L>;
   extern __shared__ __align__(32) unsigned char smem_raw[];
+  fhat += blockIdx.y * fcol;  // column of a multi-column launch
+  g += blockIdx.y * gcol;
   const int4 task = tasks[blockIdx.x];
   const int o0 = task.x * G.bs[0];
   const int P0 = G.bs[0] + L - 1;
