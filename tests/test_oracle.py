@@ -256,3 +256,27 @@ def test_direct_transposes_and_ndft_forms():
                                    oracle.ndft_forward_sep(kc, fc), rtol=1e-11)
         np.testing.assert_allclose(oracle.nndft_adjoint(kc, y, v),
                                    oracle.ndft_adjoint_sep(kc, N, v).ravel(order="F"), rtol=1e-11, atol=1e-11)
+
+
+def test_golden_tools():
+    """Regression anchors of the Toeplitz and direct-transform restatements
+    (tests/golden/tools.npz), plus the reference's own relations on them."""
+    z = np.load(os.path.join(GOLDEN, "tools.npz"))
+    N = tuple(z["N"])
+    tr, x = z["tr"], z["x"]
+    lam = oracle.toeplitz_kernel(N, tr, m=4, sigma=2.0)
+    np.testing.assert_allclose(lam, z["toeplitz_kernel_m4"], rtol=1e-12, atol=1e-9)
+    np.testing.assert_allclose(oracle.toeplitz_kernel_explicit(N, tr), z["toeplitz_kernel_explicit"],
+                               rtol=1e-12, atol=1e-9)
+    np.testing.assert_allclose(oracle.convolve_toeplitz(x, lam), z["toeplitz_product_m4"], rtol=1e-12, atol=1e-9)
+    assert _julia_isapprox(z["toeplitz_kernel_m4"], z["toeplitz_kernel_explicit"], 1e-6)  # testToeplitz.jl:17
+    kc, fr, v = z["kc"], z["fr"], z["v"]
+    np.testing.assert_allclose(oracle.ndct_forward(kc, fr), z["ndct_forward"], rtol=1e-12, atol=1e-12)
+    np.testing.assert_allclose(oracle.ndct_transpose(kc, N, v), z["ndct_transpose"], rtol=1e-12, atol=1e-12)
+    np.testing.assert_allclose(oracle.ndst_forward(kc, fr), z["ndst_forward"], rtol=1e-12, atol=1e-12)
+    Np = tuple(n + 1 for n in N)
+    np.testing.assert_allclose(oracle.ndst_transpose(kc, Np, v), z["ndst_transpose"], rtol=1e-12, atol=1e-12)
+    np.testing.assert_allclose(oracle.nndft_forward(tr[:, :60], z["y"], z["fy"]), z["nndft_forward"],
+                               rtol=1e-12, atol=1e-12)
+    np.testing.assert_allclose(oracle.nndft_adjoint(tr[:, :60], z["y"], z["ndct_forward"].astype(np.complex128)),
+                               z["nndft_adjoint"], rtol=1e-12, atol=1e-12)
