@@ -10,6 +10,6 @@ from .plan import (  # noqa: F401
     nfft_adjoint, GB300DirectionalPlan, NFFTBatch, nodes_, params_to_reltol, plan_nfft, reltol_to_params, size_in,
     size_out)
 from .trig import (  # noqa: F401
-    GB300NFCTPlan, GB300NFSTPlan, NDCTPlan, NDFTPlan, NDSTPlan, NNDFTPlan, ndct, ndct_transposed, ndft, ndft_adjoint,
-    nfct, nfct_transpose, nfst, nfst_transpose, plan_nfct, plan_nfst)
+    GB300NFCTPlan, GB300NFSTPlan, NDCTPlan, NDFTPlan, NDSTPlan, NNDFTPlan, ndct, ndct_transpose, ndct_transposed,
+    ndft, ndft_adjoint, nfct, nfct_transpose, nfst, nfst_transpose, plan_nfct, plan_nfst)
 from ._lib import LIB_PATH, exported_symbols, load  # noqa: F401

@@ -242,6 +242,10 @@ def ndct_transposed(k, N, fHat, device="cuda"):
     return NDCTPlan(k, N, device).transpose() * fHat
 
 
+# AbstractNFFTs exports the name ndct_transpose (AbstractNFFTs/src/AbstractNFFTs.jl:25)
+ndct_transpose = ndct_transposed
+
+
 # ------------------------------------------------------------ NFCT / NFST
 class _TrigPlan:
     """NFCT / NFST plan of size N on the GPU NFFT (size 2N) of the even / odd
