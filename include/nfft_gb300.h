@@ -344,6 +344,25 @@ int nfft_tplan_forward(nfft_tplan* plan, const void* f, void* fhat);
 /* mul!(f, transpose(p), fHat): real fHat (M) -> real f */
 int nfft_tplan_transpose(nfft_tplan* plan, const void* fhat, void* f);
 
+/* Fast NNFFT plans (nonequispaced in both domains: the transform of
+ * NNDFTPlan, src/direct.jl:252-287; AbstractNNFFTPlan of AbstractNFFTs):
+ * fHat_j = sum_l c_l exp(-2 pi i k_j . y_l) with nodes k (D x M, |k| <= 1/2)
+ * and points y (D x Ny, any finite values).  Computed by spreading c at y / N1
+ * with a plan of size N1 = 2 ceil(max |y| + m / sigma) + 2, a forward NFFT of
+ * size sigma N1 at k / sigma1 and a division by the window transform; params
+ * as for nfft_plan_create.  nfft_nnplan_set_nodes (re)builds the two plans
+ * and synchronises. */
+typedef struct nfft_nnplan nfft_nnplan;
+int nfft_nnplan_create(nfft_nnplan** plan, int precision, int D, int64_t M, int64_t Ny, const nfft_params* params,
+                       void* stream);
+int nfft_nnplan_destroy(nfft_nnplan* plan);
+int nfft_nnplan_set_stream(nfft_nnplan* plan, void* stream);
+int nfft_nnplan_set_nodes(nfft_nnplan* plan, const void* k, const void* y, int on_device);
+/* c (Ny complex) -> fhat (M complex) */
+int nfft_nnplan_forward(nfft_nnplan* plan, const void* c, void* fhat);
+/* fhat (M complex) -> c (Ny complex) */
+int nfft_nnplan_adjoint(nfft_nnplan* plan, const void* fhat, void* c);
+
 /* Wait for the plan's stream. */
 int nfft_sync(nfft_plan* plan);
 

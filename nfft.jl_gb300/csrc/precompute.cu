@@ -75,59 +75,7 @@ __global__ void build_weight_table_kernel(Geom<T> G, const T* __restrict__ frac4
 }
 
 // ---------------------------------------------------------------- phi-hat
-
-__device__ double window_hat(int window, double n, double Nt, int m, double sigma) {
-  const double PI = 3.14159265358979323846;
-  switch (window) {
-    case NFFT_WINDOW_KAISER_BESSEL: {  // src/windowFunctions.jl:36-39
-      double b = PI * (2.0 - 1.0 / sigma);
-      double a = 2.0 * PI * n / Nt;
-      return bessel_i0_series<double>(m * sqrt(b * b - a * a));
-    }
-    case NFFT_WINDOW_GAUSS: {  // :70-73
-      double b = m / PI;
-      double a = PI * n / Nt;
-      return exp(-(a * a) * b);
-    }
-    case NFFT_WINDOW_SPLINE: {  // :98-100, Julia sinc(x) = sin(pi x)/(pi x)
-      double x = n / Nt;
-      double s = (x == 0.0) ? 1.0 : sin(PI * x) / (PI * x);
-      double r = 1.0;
-      for (int i = 0; i < 2 * m; ++i) r *= s;
-      return r;
-    }
-    case NFFT_WINDOW_KAISER_BESSEL_REV: {  // :51-57, real(sinc(sqrt(complex(a2))/pi))
-      double b = PI * (2.0 - 1.0 / sigma);
-      double u = 2.0 * PI * m * n / Nt;
-      double a2 = u * u - (m * b) * (m * b);
-      if (a2 > 0.0) {
-        double a = sqrt(a2);
-        return sin(a) / a;
-      } else if (a2 < 0.0) {
-        double a = sqrt(-a2);
-        return sinh(a) / a;
-      }
-      return 1.0;
-    }
-    case NFFT_WINDOW_COSH_TYPE: {  // :118-134
-      double beta = PI * m * (2.0 - 1.0 / sigma);
-      double gamma = beta / (2.0 * PI);
-      double zeta = PI / (cosh(beta) - 1.0) * m;
-      double arg = m * n / Nt;
-      double aa = fabs(arg);
-      double j0 = bessel_j0_series<double>(2.0 * PI * arg);
-      if (aa < gamma) {
-        double q = 2.0 * PI * arg;
-        return zeta * (bessel_i0_series<double>(sqrt(beta * beta - q * q)) - j0);
-      } else if (aa > gamma) {
-        double q = 2.0 * PI * arg;
-        return zeta * (bessel_j0_series<double>(sqrt(q * q - beta * beta)) - j0);
-      }
-      return zeta * (1.0 - bessel_j0_series<double>(beta));
-    }
-  }
-  return 1.0;
-}
+// window_hat (nfft_internal.cuh)
 
 // precomputeWindowHatInvLUT (src/precomputation.jl:347-358), FP64: per
 // dimension a 30-point first-kind Chebyshev interpolant of

@@ -543,6 +543,67 @@ function LinearAlgebra.mul!(f::CuArray{T,D}, pl::Transpose{T,<:GB300TrigPlan{T,D
   return f
 end
 
+# ---------------------------------------------------------------- NNFFT plans
+
+"""
+    plan_nnfft(CuArray, k, y; m, σ, window, ...)
+
+Fast NNFFT (AbstractNNFFTPlan; the transform of NNDFTPlan): nodes k (D x J,
+|k| <= 1/2), points y (D x N).  Spreading at y / N1, a forward NFFT of size
+σ N1 at k / σ1 and a division by the window transform (`nfft_nnplan_*`).
+"""
+mutable struct GB300NNFFTPlan{T,D} <: AbstractNNFFTPlan{T,1,1}
+  handle::Ptr{Cvoid}
+  J::Int
+  N::Int
+  k::Matrix{T}
+  y::Matrix{T}
+end
+
+function AbstractNFFTs.plan_nnfft(::GB300Backend, ::Type{<:CuArray}, k::Matrix{T}, y::Matrix{T}, rest...;
+                                  window::Symbol=:kaiser_bessel, precompute=AbstractNFFTs.POLYNOMIAL,
+                                  blocking::Bool=true, kwargs...) where {T<:Union{Float32,Float64}}
+  D = size(k, 1)
+  size(y, 1) == D || throw(ArgumentError("Nodes k have dimension $D != $(size(y, 1)) of the points y"))
+  m, σ, reltol = AbstractNFFTs.accuracyParams(; kwargs...)
+  cp = CParams(m, σ, WINDOWS[window], Int(precompute), blocking, false, false, (0, 0, 0), 0, 0)
+  h = Ref{Ptr{Cvoid}}(C_NULL)
+  check(ccall((:nfft_nnplan_create, libnfft[]), Cint,
+              (Ref{Ptr{Cvoid}}, Cint, Cint, Int64, Int64, Ref{CParams}, Ptr{Cvoid}),
+              h, T == Float32 ? 32 : 64, D, size(k, 2), size(y, 2), cp, CUDA.stream().handle))
+  p = GB300NNFFTPlan{T,D}(h[], size(k, 2), size(y, 2), k, y)
+  finalizer(p) do q
+    q.handle == C_NULL || ccall((:nfft_nnplan_destroy, libnfft[]), Cint, (Ptr{Cvoid},), q.handle)
+    q.handle = C_NULL
+  end
+  check(ccall((:nfft_nnplan_set_nodes, libnfft[]), Cint, (Ptr{Cvoid}, Ptr{T}, Ptr{T}, Cint), p.handle, k, y, 0))
+  return p
+end
+
+AbstractNFFTs.size_in(p::GB300NNFFTPlan) = (p.N,)
+AbstractNFFTs.size_out(p::GB300NNFFTPlan) = (p.J,)
+
+bind_stream!(p::GB300NNFFTPlan) =
+  check(ccall((:nfft_nnplan_set_stream, libnfft[]), Cint, (Ptr{Cvoid}, Ptr{Cvoid}), p.handle, CUDA.stream().handle))
+
+function LinearAlgebra.mul!(fHat::CuVector{Complex{T}}, p::GB300NNFFTPlan{T}, c::CuVector{Complex{T}}) where {T}
+  length(c) == p.N && length(fHat) == p.J || throw(DimensionMismatch("Data is not consistent with the plan"))
+  bind_stream!(p)
+  check(ccall((:nfft_nnplan_forward, libnfft[]), Cint, (Ptr{Cvoid}, CuPtr{Complex{T}}, CuPtr{Complex{T}}),
+              p.handle, c, fHat))
+  return fHat
+end
+
+function LinearAlgebra.mul!(c::CuVector{Complex{T}}, pl::Adjoint{Complex{T},<:GB300NNFFTPlan{T}},
+                            fHat::CuVector{Complex{T}}) where {T}
+  p = pl.parent
+  length(c) == p.N && length(fHat) == p.J || throw(DimensionMismatch("Data is not consistent with the plan"))
+  bind_stream!(p)
+  check(ccall((:nfft_nnplan_adjoint, libnfft[]), Cint, (Ptr{Cvoid}, CuPtr{Complex{T}}, CuPtr{Complex{T}}),
+              p.handle, fHat, c))
+  return c
+end
+
 # ---------------------------------------------------------------- direct transforms (src/direct.jl)
 
 """

@@ -11,5 +11,6 @@ from .plan import (  # noqa: F401
     size_out)
 from .trig import (  # noqa: F401
     GB300NFCTPlan, GB300NFSTPlan, NDCTPlan, NDFTPlan, NDSTPlan, NNDFTPlan, ndct, ndct_transpose, ndct_transposed,
-    ndft, ndft_adjoint, nfct, nfct_transpose, nfst, nfst_transpose, plan_nfct, plan_nfst)
+    ndft, ndft_adjoint, nfct, nfct_transpose, nfst, nfst_transpose, plan_nfct, plan_nfst, GB300NNFFTPlan,
+    plan_nnfft)
 from ._lib import LIB_PATH, exported_symbols, load  # noqa: F401

@@ -115,6 +115,12 @@ SIGNATURES = {
     "nfft_tplan_set_nodes": (_I, [_P, _P, _I]),
     "nfft_tplan_forward": (_I, [_P, _P, _P]),
     "nfft_tplan_transpose": (_I, [_P, _P, _P]),
+    "nfft_nnplan_create": (_I, [ctypes.POINTER(_P), _I, _I, _I64, _I64, ctypes.POINTER(nfft_params), _P]),
+    "nfft_nnplan_destroy": (_I, [_P]),
+    "nfft_nnplan_set_stream": (_I, [_P, _P]),
+    "nfft_nnplan_set_nodes": (_I, [_P, _P, _P, _I]),
+    "nfft_nnplan_forward": (_I, [_P, _P, _P]),
+    "nfft_nnplan_adjoint": (_I, [_P, _P, _P]),
     "nfft_kernel_launch_count": (_I64, []),
     "nfft_status_string": (ctypes.c_char_p, [_I]),
     "nfft_last_error": (ctypes.c_char_p, []),

@@ -1,5 +1,8 @@
 """Direct transforms and NFCT / NFST plans on the GPU.
 
+Also a fast NNFFT plan (``plan_nnfft`` / ``GB300NNFFTPlan``: the transform of
+``NNDFTPlan`` computed with two NFFT plans, ``nfft_nnplan_*``).
+
 Mirrors NFFT.jl's direct plans (src/direct.jl: ``NDFTPlan``, ``NDCTPlan``,
 ``NDSTPlan``, ``NNDFTPlan`` with ``ndft``, ``ndft_adjoint``, ``ndct``,
 ``ndct_transposed``) and AbstractNFFTs' NFCT / NFST interface
@@ -433,3 +436,137 @@ def nfst(k, f, **kw):
 def nfst_transpose(k, N, fHat, **kw):
     """nfst_transpose(k, N, fHat) (derived.jl:146-149): N is the plan size."""
     return plan_nfst(k, N, **kw).transpose() * fHat
+
+
+# ------------------------------------------------------------------ NNFFT
+class GB300NNFFTPlan:
+    """Fast NNFFT (AbstractNNFFTPlan; the transform of NNDFTPlan,
+    src/direct.jl:252-287): fHat_j = sum_l c_l exp(-2 pi i k_j . y_l) with nodes
+    k (D x J, |k| <= 1/2) and points y (D x N).  Computed by spreading c at
+    y / N1, a forward NFFT of size sigma N1 at k / sigma1 and a division by the
+    window transform (``nfft_nnplan_*``); accuracy as an NFFT with m, sigma."""
+
+    def __init__(self, k, y, *, m=None, sigma=None, reltol=None, window="kaiser_bessel",
+                 precompute=P.PrecomputeFlags.POLYNOMIAL, blocking=True, device="cuda", **_):
+        self.device = _device(device)
+        kk = P.GB300NFFTPlan._nodes_array(k)
+        yy = P.GB300NFFTPlan._nodes_array(y)
+        if kk.shape[0] != yy.shape[0]:
+            raise P.ArgumentError(f"Nodes k have dimension {kk.shape[0]} != {yy.shape[0]} of the points y")
+        if kk.shape[0] > 3:
+            raise NotImplementedError("NNFFT plans support D <= 3")
+        if window not in P.WINDOWS:
+            raise NotImplementedError(f"Window {window} not yet implemented!")
+        m_, s_, r_ = P.accuracy_params(m, sigma, reltol)
+        self.dtype = torch.float32 if kk.dtype in (np.float32, torch.float32) else torch.float64
+        self.cdtype = torch.complex64 if self.dtype == torch.float32 else torch.complex128
+        self.precision = 32 if self.dtype == torch.float32 else 64
+        self.D, self.J = kk.shape
+        self.N = int(yy.shape[1])
+        self.params = P.NFFTParams(m=m_, sigma=s_, reltol=r_, window=window,
+                                   precompute=P.PrecomputeFlags(precompute), blocking=bool(blocking))
+        lib = L.load()
+        prm = L.nfft_params()
+        lib.nfft_params_default(ctypes.byref(prm))
+        prm.m = m_
+        prm.sigma = s_
+        prm.window = P.WINDOWS[window]
+        prm.precompute = int(precompute)
+        prm.blocking = int(bool(blocking))
+        h = ctypes.c_void_p()
+        self._handle = None
+        with torch.cuda.device(self.device):
+            stream = torch.cuda.current_stream(self.device).cuda_stream
+            P._check(lib.nfft_nnplan_create(ctypes.byref(h), self.precision, self.D, int(self.J), self.N,
+                                            ctypes.byref(prm), ctypes.c_void_p(stream)))
+        self._handle = h
+        self._stream = stream
+        self.nodes_(kk, yy)
+
+    def __del__(self):
+        h = getattr(self, "_handle", None)
+        if h is not None and h.value:
+            try:
+                L.load().nfft_nnplan_destroy(h)
+            except Exception:
+                pass
+            self._handle = None
+
+    def _sync_stream(self):
+        s = torch.cuda.current_stream(self.device).cuda_stream
+        if s != self._stream:
+            P._check(L.load().nfft_nnplan_set_stream(self._handle, ctypes.c_void_p(s)))
+            self._stream = s
+
+    def size_in(self):
+        return (self.N,)
+
+    def size_out(self):
+        return (self.J,)
+
+    def nodes_(self, k, y):
+        """nodes!(p, k) with the points y."""
+        kk = P.GB300NFFTPlan._nodes_array(k)
+        yy = P.GB300NFFTPlan._nodes_array(y)
+        if kk.shape != (self.D, self.J) or yy.shape != (self.D, self.N):
+            raise P.DimensionMismatch(f"nodes must be {self.D} x {self.J} and points {self.D} x {self.N}")
+        npdt = np.float32 if self.precision == 32 else np.float64
+        kc = np.ascontiguousarray((kk.cpu().numpy() if isinstance(kk, torch.Tensor) else kk).T.astype(npdt))
+        yc = np.ascontiguousarray((yy.cpu().numpy() if isinstance(yy, torch.Tensor) else yy).T.astype(npdt))
+        self._sync_stream()
+        P._check(L.load().nfft_nnplan_set_nodes(self._handle, ctypes.c_void_p(kc.ctypes.data),
+                                                 ctypes.c_void_p(yc.ctypes.data), 0))
+        self.k, self.y = kk, yy
+        return self
+
+    def _vec(self, v, n, what):
+        if not isinstance(v, torch.Tensor) or tuple(v.shape) != (n,):
+            raise P.DimensionMismatch(f"{what} is not consistent with the NNFFT plan")
+        if v.dtype != self.cdtype or v.device != self.device or not v.is_contiguous():
+            raise P.ArgumentError(f"{what} must be a contiguous {self.cdtype} tensor on {self.device}")
+        return v
+
+    def forward_(self, fHat, c):
+        """mul!(fHat, p, c)."""
+        c = self._vec(c, self.N, "input")
+        fHat = self._vec(fHat, self.J, "output")
+        self._sync_stream()
+        P._check(L.load().nfft_nnplan_forward(self._handle, P._ptr(c), P._ptr(fHat)))
+        return fHat
+
+    def adjoint_(self, c, fHat):
+        """mul!(c, adjoint(p), fHat)."""
+        c = self._vec(c, self.N, "output")
+        fHat = self._vec(fHat, self.J, "input")
+        self._sync_stream()
+        P._check(L.load().nfft_nnplan_adjoint(self._handle, P._ptr(fHat), P._ptr(c)))
+        return c
+
+    def _to_vec(self, v):
+        if not isinstance(v, torch.Tensor):
+            v = torch.as_tensor(np.asarray(v))
+        return v.to(device=self.device, dtype=self.cdtype).contiguous()
+
+    def __mul__(self, c):
+        fHat = torch.empty(self.J, dtype=self.cdtype, device=self.device)
+        return self.forward_(fHat, self._to_vec(c))
+
+    def _backward_mul(self, fHat):
+        c = torch.empty(self.N, dtype=self.cdtype, device=self.device)
+        return self.adjoint_(c, self._to_vec(fHat))
+
+    def adjoint(self):
+        return _AdjointOf(self)
+
+    @property
+    def H(self):
+        return _AdjointOf(self)
+
+
+def plan_nnfft(*args, **kwargs):
+    """plan_nnfft([CuArray,] k, y; m, σ, window, ...) (AbstractNFFTs/src/derived.jl:39-42)."""
+    if args and (isinstance(args[0], type) or args[0] is None):
+        args = args[1:]
+    if "σ" in kwargs:
+        kwargs["sigma"] = kwargs.pop("σ")
+    return GB300NNFFTPlan(args[0], args[1], **kwargs)

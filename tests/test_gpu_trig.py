@@ -195,3 +195,26 @@ def test_ndst_with_single_point_dimension():
     assert rel(host(p * f), oracle.ndst_forward(k, f)) < 1e-12
     q = nf.plan_nfst(k, N, m=5, sigma=2.0)
     assert rel(host(q * f), oracle.ndst_forward(k, f)) < 1e-7
+
+
+@pytest.mark.parametrize("D", [1, 2, 3])
+@pytest.mark.parametrize("m,tol", [(4, 1e-6), (6, 1e-9)])
+def test_nnfft_vs_nndft(D, m, tol):
+    """Fast NNFFT against the NNDFT (test/wrappers.jl:70-96 shapes: J = N = 40,
+    y in [-5, 5)^D); FP64, forward and adjoint."""
+    rng = np.random.default_rng(10 * D + m)
+    J, Ny = 40, 40
+    k = rng.random((D, J)) - 0.5
+    y = (rng.random((D, Ny)) - 0.5) * 10
+    p = nf.plan_nnfft(k, y, m=m, sigma=2.0)
+    c = rng.standard_normal(Ny) + 1j * rng.standard_normal(Ny)
+    fh = rng.standard_normal(J) + 1j * rng.standard_normal(J)
+    assert rel(host(p * c), oracle.nndft_forward(k, y, c)) < tol
+    assert rel(host(p.adjoint() * fh), oracle.nndft_adjoint(k, y, fh)) < tol
+    # larger point clouds and FP32
+    k2 = (rng.random((D, 3000)) - 0.5).astype(np.float32)
+    y2 = ((rng.random((D, 2000)) - 0.5) * 40).astype(np.float32)
+    q = nf.plan_nnfft(k2, y2, m=4, sigma=2.0)
+    c2 = (rng.standard_normal(2000) + 1j * rng.standard_normal(2000)).astype(np.complex64)
+    ref = nf.NNDFTPlan(k2, y2) * c2
+    assert rel(host(q * c2), host(ref)) < 1e-5
