@@ -79,3 +79,13 @@ def test_julia_backend_binds_the_interface_entry_points():
     for n in declared_functions():
         if n not in helpers:
             assert f":{n}" in jl, n
+
+
+def test_build_compiles_every_source():
+    """build() compiles every CUDA source of the package (a file missing from
+    the list would silently drop its entry points on the GPU machine)."""
+    import sys
+    sys.path.insert(0, os.path.join(ROOT, "nfft.jl_gb300"))
+    import build as B
+    on_disk = sorted(f for f in os.listdir(B.CSRC) if f.endswith(".cu"))
+    assert sorted(B.SOURCES) == on_disk
