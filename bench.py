@@ -168,32 +168,38 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(rows), "window": window}
 
 
-def ndft_forward_subset(k64, f, sub):
-    """Direct NDFT (src/direct.jl:99-123) in FP64 at the nodes `sub`:
-    fHat_j = sum_n f[n] exp(-2 pi i k_j . (n - N/2)), separable per node."""
-    N = f.shape
-    fc = np.asarray(f, np.complex128)
-    out = np.empty(len(sub), np.complex128)
-    for i, j in enumerate(sub):
-        t = fc
-        for d in reversed(range(len(N))):  # contract the last axis first
-            e = np.exp(-2j * np.pi * k64[d, j] * (np.arange(N[d]) - N[d] // 2))
-            t = t @ e if t.ndim > 1 else t.dot(e)
-        out[i] = t
-    return out
+N_ERR_NODES = 4096  # random nodes of the forward error subset
+N_ERR_FREQS = 4096  # random output frequencies of the adjoint error subset
 
 
-def ndft_adjoint_subset(k64, N, fhat, lin):
-    """Direct adjoint NDFT (src/direct.jl:126-151) in FP64 at the column-major
-    linear output indices `lin`."""
-    fh = np.asarray(fhat, np.complex128)
-    out = np.empty(len(lin), np.complex128)
-    for i, q in enumerate(lin):
-        ph = np.zeros(k64.shape[1])
-        for d, n_d in enumerate(np.unravel_index(int(q), N, order="F")):
-            ph += k64[d] * (n_d - N[d] // 2)
-        out[i] = np.sum(fh * np.exp(2j * np.pi * ph))
-    return out
+def error_subsets(M, n_img, seed=7):
+    """Random node indices (forward) and column-major output indices (adjoint)
+    of the error measurement, sorted."""
+    rng = np.random.default_rng(seed)
+    return (np.sort(rng.choice(M, min(M, N_ERR_NODES), replace=False)),
+            np.sort(rng.choice(n_img, min(n_img, N_ERR_FREQS), replace=False)))
+
+
+def frequencies(N, lin):
+    """Integer frequencies n - N div 2 (D x len(lin)) of column-major linear indices."""
+    idx = np.unravel_index(np.asarray(lin), tuple(N), order="F")
+    return np.stack([i - n // 2 for i, n in zip(idx, N)]).astype(np.float64)
+
+
+def ndft_reference_subsets(k64, f, fhat, sub, lin, device="cuda"):
+    """FP64 NDFT (src/direct.jl:99-151) of the inputs at the nodes `sub`
+    (forward) and at the column-major output indices `lin` (adjoint), by this
+    library's exact direct GPU sums: an NDFT plan of the node subset (forward),
+    and the adjoint of an NNDFT plan from all nodes to the frequencies
+    n - N div 2 (f[n] = sum_j fHat_j exp(2 pi i k_j . n)).  The tests check
+    these sums against the oracle's NDFT on the same subsets."""
+    import nfftgb300 as nf
+    N = tuple(f.shape)
+    pf = nf.NDFTPlan(np.ascontiguousarray(k64[:, sub]), N, device)
+    ref_f = (pf * np.asarray(f, np.complex128)).cpu().numpy()
+    pa = nf.NNDFTPlan(np.ascontiguousarray(k64), frequencies(N, lin), device)
+    ref_a = (pa.adjoint() * np.asarray(fhat, np.complex128)).cpu().numpy()
+    return ref_f, ref_a
 
 
 def rel_l2(x, ref):
@@ -202,17 +208,15 @@ def rel_l2(x, ref):
     return float(np.linalg.norm(x - ref) / np.linalg.norm(ref))
 
 
-def rel_err_subset(k64, f, fhat, y, x, n_fwd=48, n_adj=24, seed=7):
-    """Relative l2 errors of the GPU outputs on node / frequency subsets
-    against the FP64 NDFT."""
-    rng = np.random.default_rng(seed)
-    M = k64.shape[1]
-    sub = rng.choice(M, n_fwd, replace=False)
-    e_fwd = rel_l2(y[sub], ndft_forward_subset(k64, f, sub))
-    N = f.shape
-    lin = rng.choice(int(np.prod(N)), n_adj, replace=False)
-    e_adj = rel_l2(x.ravel(order="F")[lin], ndft_adjoint_subset(k64, N, fhat, lin))
-    return e_fwd, e_adj
+def rel_err_subset(k64, f, fhat, y, x, seed=7):
+    """Relative l2 errors of the GPU outputs against the FP64 NDFT on 4096
+    random nodes (forward) and 4096 random output frequencies (adjoint)."""
+    sub, lin = error_subsets(k64.shape[1], int(np.prod(f.shape)), seed)
+    ref_f, ref_a = ndft_reference_subsets(k64, f, fhat, sub, lin)
+    return {"forward": rel_l2(y[sub], ref_f), "adjoint": rel_l2(x.ravel(order="F")[lin], ref_a),
+            "nodes": int(len(sub)), "frequencies": int(len(lin)),
+            "reference": "exact FP64 sums (NDFT of the node subset, NNDFT adjoint at the frequency subset) "
+                         "on the GPU, checked against the oracle's NDFT in the tests"}
 
 
 def max_over_ranks(t, world, device):
@@ -417,13 +421,12 @@ def run_ours(args):
     d2h = y_pin.numel() * 8 + x_pin.numel() * 8
 
     # ---- accuracy of this run's outputs (outside the timed region)
-    err_fwd = err_adj = None
+    err = None
     if rank == 0 and not args.no_check:
         p.forward_(y, f)
         p.adjoint_(x, fhat)
-        err_fwd, err_adj = rel_err_subset(k.astype(np.float64), f_h.astype(np.complex128),
-                                          fhat_h.astype(np.complex128), y.cpu().numpy(),
-                                          x.cpu().numpy())
+        err = rel_err_subset(k.astype(np.float64), f_h.astype(np.complex128), fhat_h.astype(np.complex128),
+                             y.cpu().numpy(), x.cpu().numpy())
 
     # ---- the plain FP64 path on the same workload (comparator)
     plain = None
@@ -502,7 +505,7 @@ def run_ours(args):
             "roofline": roofline,
             "pair_hbm_gbs": pair_gbs,
             "stages_ms": stages,
-            "rel_err_vs_fp64_ndft": {"forward": err_fwd, "adjoint": err_adj},
+            "rel_err_vs_fp64_ndft": err,
             "plain_fp64_path": plain,
             "cpu_baseline": cpu,
             "clocks": clk.summary(),
@@ -670,12 +673,8 @@ def run_config(args):
     t_ours = timed(step, args.steps, args.warmup)
     launches = (nf.kernel_launch_count() - l0) // (args.steps + args.warmup)
     yo, xo = y.cpu().numpy(), x.cpu().numpy()
-    rs = np.random.default_rng(7)
-    sub = rs.choice(M, min(M, 48), replace=False)
-    lin = rs.choice(int(np.prod(N)), 24, replace=False)
     k64 = k.astype(np.float64)
-    err = {"forward": rel_l2(yo[sub], ndft_forward_subset(k64, f_h, sub)),
-           "adjoint": rel_l2(xo.ravel(order="F")[lin], ndft_adjoint_subset(k64, N, fh_h, lin))}
+    err = rel_err_subset(k64, f_h, fh_h, yo, xo)
     line = {"metric": f"{args.workload}: fwd+adj{'+dk' if grad else ''} NFFT nodes/s", "value": M / t_ours,
             "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": t_ours * 1e3, "higher_is_better": True, "dtype": "f32" if cfg["prec"] == 32 else "f64",
@@ -970,11 +969,8 @@ def run_extras(args):
     y = torch.empty(M, dtype=torch.complex64, device=dev)
     x = nf.empty_image(N3, torch.complex64, dev)
     k64 = k.astype(np.float64)
-    rs = np.random.default_rng(7)
-    sub = rs.choice(M, 32, replace=False)
-    lin = rs.choice(int(np.prod(N3)), 16, replace=False)
-    ref_f = ndft_forward_subset(k64, f_h, sub)
-    ref_a = ndft_adjoint_subset(k64, N3, fh_h, lin)
+    sub, lin = error_subsets(M, int(np.prod(N3)))
+    ref_f, ref_a = ndft_reference_subsets(k64, f_h, fh_h, sub, lin)
     table = {}
     for window in ("kaiser_bessel", "gauss", "spline", "kaiser_bessel_rev", "cosh_type"):
         for pre in ("TENSOR", "POLYNOMIAL", "LINEAR", "FULL"):

@@ -440,52 +440,240 @@ double oracle_window_phi(int win, double x, double Nt, int m, double sigma) {
 
 ORACLE_API(f32, float)
 ORACLE_API(f64, double)
+}  // extern "C"
 
 // Direct NDFT forward on a subset of nodes, src/direct.jl:99-123:
-// fhat[j] = sum_n f[n] exp(-2 pi i k_j . (n - N÷2)).  The D-dimensional sum
-// is factored dimension by dimension (separable phases), in FP64.
+// fhat[j] = sum_n f[n] exp(-2 pi i k_j . (n - N÷2)), in FP64.
+//
+// The D-dimensional sum is contracted one (virtual) dimension at a time with
+// per-node phase tables (separable phases).  A dimension longer than 4096 is
+// split into two virtual dimensions n = v + B u (B = 2048), whose phases are
+// exp(-2 pi i k (v - N÷2)) and exp(-2 pi i k B u), so a 1-D image of 2^22
+// points needs tables of 2 x 2048 entries per node.  Nodes are processed in
+// blocks of 8 so that each image row is read once per block.
+namespace {
+
+constexpr int kMaxV = 6;
+
+struct VDims {
+  int nv = 0;
+  int64_t n[kMaxV];      // virtual extents, fastest first
+  int dim[kMaxV];        // source dimension of the virtual dimension
+  double scale[kMaxV];   // image coordinate = scale * i + off
+  double off[kMaxV];
+};
+
+// Split the image dimensions into virtual dimensions of at most `maxlen` points
+// (a longer extent must be divisible by the chosen base).
+VDims make_vdims(int D, const int64_t* N, int64_t maxlen, int64_t base) {
+  VDims V;
+  for (int d = 0; d < D; ++d) {
+    int64_t rest = N[d];
+    double sc = 1.0, of = -double(N[d] / 2);
+    while (rest > maxlen && rest % base == 0) {
+      V.n[V.nv] = base; V.dim[V.nv] = d; V.scale[V.nv] = sc; V.off[V.nv] = of; ++V.nv;
+      sc *= double(base); of = 0.0; rest /= base;
+    }
+    V.n[V.nv] = rest; V.dim[V.nv] = d; V.scale[V.nv] = sc; V.off[V.nv] = of; ++V.nv;
+  }
+  return V;
+}
+
+// exp(sign 2 pi i x t) for t = scale*i + off, i = 0..n-1, written to (c[i*stride], s[i*stride]).
+// Exact seeds every 32 entries (fractional part of x*t formed with an FMA
+// residual), complex multiplication by exp(sign 2 pi i x scale) in between
+// (relative error below 1e-14).
+void phase_table(double x, double sign, double scale, double off, int64_t n, double* c, double* s, int64_t stride) {
+  auto seed = [&](double t, double& cr, double& ci) {
+    const double p = x * t;
+    const double e = std::fma(x, t, -p);
+    const double fr = (p - std::nearbyint(p)) + e;
+    cr = std::cos(2.0 * PI * fr);
+    ci = sign * std::sin(2.0 * PI * fr);
+  };
+  double wr, wi;
+  seed(scale, wr, wi);
+  for (int64_t i0 = 0; i0 < n; i0 += 32) {
+    double cr, ci;
+    seed(scale * double(i0) + off, cr, ci);
+    const int64_t i1 = std::min<int64_t>(n, i0 + 32);
+    for (int64_t i = i0; i < i1; ++i) {
+      c[i * stride] = cr;
+      s[i * stride] = ci;
+      const double t = cr * wr - ci * wi;
+      ci = cr * wi + ci * wr;
+      cr = t;
+    }
+  }
+}
+
+}  // namespace
+
+extern "C" {
 void oracle_ndft_forward(int D, const int64_t* N, int64_t Msel, const double* k, const double* f,
                          double* out) {
-  int64_t n3[3] = {1, 1, 1};
-  for (int d = 0; d < D; ++d) n3[d] = N[d];
+  constexpr int NB = 8;
+  const VDims V = make_vdims(D, N, 4096, 2048);
+  int64_t rows = 1;
+  for (int v = 1; v < V.nv; ++v) rows *= V.n[v];
+  const int64_t n0 = V.n[0];
+  const int64_t nblk = (Msel + NB - 1) / NB;
 #pragma omp parallel
   {
-    std::vector<double> ph[3];
-    for (int d = 0; d < 3; ++d) ph[d].resize(2 * n3[d]);
-    std::vector<double> acc1(2 * n3[1] * n3[2]);
-#pragma omp for schedule(dynamic, 1)
-    for (int64_t j = 0; j < Msel; ++j) {
-      for (int d = 0; d < 3; ++d) {
-        for (int64_t n = 0; n < n3[d]; ++n) {
-          if (d >= D) { ph[d][2 * n] = 1.0; ph[d][2 * n + 1] = 0.0; continue; }
-          const double arg = -2.0 * PI * k[d + D * j] * double(n - n3[d] / 2);
-          ph[d][2 * n] = std::cos(arg);
-          ph[d][2 * n + 1] = std::sin(arg);
-        }
-      }
-      double sr = 0, si = 0;
-      for (int64_t i2 = 0; i2 < n3[2]; ++i2) {
-        double r2 = 0, q2 = 0;
-        for (int64_t i1 = 0; i1 < n3[1]; ++i1) {
-          const double* fr = f + 2 * n3[0] * (i1 + n3[1] * i2);
-          double r1 = 0, q1 = 0;
-          for (int64_t i0 = 0; i0 < n3[0]; ++i0) {
-            const double a = fr[2 * i0], b = fr[2 * i0 + 1];
-            const double c = ph[0][2 * i0], s = ph[0][2 * i0 + 1];
-            r1 += a * c - b * s;
-            q1 += a * s + b * c;
-          }
-          const double c = ph[1][2 * i1], s = ph[1][2 * i1 + 1];
-          r2 += r1 * c - q1 * s;
-          q2 += r1 * s + q1 * c;
-        }
-        const double c = ph[2][2 * i2], s = ph[2][2 * i2 + 1];
-        sr += r2 * c - q2 * s;
-        si += r2 * s + q2 * c;
-      }
-      out[2 * j] = sr;
-      out[2 * j + 1] = si;
+    std::vector<double> tc[kMaxV], ts[kMaxV];
+    for (int v = 0; v < V.nv; ++v) {
+      tc[v].assign(V.n[v] * NB, 0.0);
+      ts[v].assign(V.n[v] * NB, 0.0);
     }
+#pragma omp for schedule(dynamic, 1)
+    for (int64_t b = 0; b < nblk; ++b) {
+      const int64_t j0 = b * NB;
+      const int nb = int(std::min<int64_t>(NB, Msel - j0));
+      for (int v = 0; v < V.nv; ++v)
+        for (int jj = 0; jj < NB; ++jj) {
+          if (jj < nb) {
+            phase_table(k[V.dim[v] + int64_t(D) * (j0 + jj)], -1.0, V.scale[v], V.off[v], V.n[v],
+                        tc[v].data() + jj, ts[v].data() + jj, NB);
+          } else {
+            for (int64_t i = 0; i < V.n[v]; ++i) tc[v][i * NB + jj] = ts[v][i * NB + jj] = 0.0;
+          }
+        }
+      // acc[v] holds the partial sum over virtual dimensions < v of the current row
+      double ar[kMaxV][NB] = {}, ai[kMaxV][NB] = {};
+      int64_t idx[kMaxV] = {};
+      for (int64_t r = 0; r < rows; ++r) {
+        const double* fr = f + 2 * n0 * r;
+        double r1[NB] = {}, q1[NB] = {};
+        for (int64_t i0 = 0; i0 < n0; ++i0) {
+          const double a = fr[2 * i0], bb = fr[2 * i0 + 1];
+          const double* cc = &tc[0][i0 * NB];
+          const double* ss = &ts[0][i0 * NB];
+          for (int jj = 0; jj < NB; ++jj) {
+            r1[jj] += a * cc[jj] - bb * ss[jj];
+            q1[jj] += a * ss[jj] + bb * cc[jj];
+          }
+        }
+        for (int jj = 0; jj < NB; ++jj) {
+          ar[0][jj] = r1[jj];
+          ai[0][jj] = q1[jj];
+        }
+        // fold level v into level v+1 while the odometer wraps
+        int v = 1;
+        for (; v < V.nv; ++v) {
+          const double* cc = &tc[v][idx[v] * NB];
+          const double* ss = &ts[v][idx[v] * NB];
+          for (int jj = 0; jj < NB; ++jj) {
+            ar[v][jj] += ar[v - 1][jj] * cc[jj] - ai[v - 1][jj] * ss[jj];
+            ai[v][jj] += ar[v - 1][jj] * ss[jj] + ai[v - 1][jj] * cc[jj];
+            ar[v - 1][jj] = ai[v - 1][jj] = 0.0;
+          }
+          if (++idx[v] < V.n[v]) break;
+          idx[v] = 0;
+        }
+      }
+      const int top = V.nv - 1;
+      for (int jj = 0; jj < nb; ++jj) {
+        out[2 * (j0 + jj)] = ar[top][jj];
+        out[2 * (j0 + jj) + 1] = ai[top][jj];
+      }
+    }
+  }
+}
+
+// Direct adjoint NDFT at selected outputs, src/direct.jl:126-151:
+// f[n] = sum_j fhat[j] exp(+2 pi i k_j . (n - N÷2)) for the column-major
+// linear indices sel, in FP64.  The phase of a (node, output) pair is a
+// product of per-node table entries, one per virtual dimension of at most
+// 256 points (n = v + 256 u + 256^2 w ...), so each pair costs a few complex
+// products.  Threads take blocks of 64 nodes, build the blocks' tables
+// (node index fastest) and add every selected output's sum over the block
+// to a private accumulator; the accumulators are added in thread order.
+void oracle_ndft_adjoint_sel(int D, const int64_t* N, int64_t M, const double* k, const double* fhat,
+                             int64_t nsel, const int64_t* sel, double* out) {
+  constexpr int NB = 64;
+  const VDims V = make_vdims(D, N, 256, 256);
+  std::vector<int32_t> vidx(size_t(nsel) * V.nv);
+  for (int64_t s = 0; s < nsel; ++s) {
+    int64_t r = sel[s];
+    for (int v = 0; v < V.nv; ++v) {
+      vidx[s * V.nv + v] = int32_t(r % V.n[v]);
+      r /= V.n[v];
+    }
+  }
+  const int nth = omp_get_max_threads();
+  std::vector<double> part(size_t(nth) * 2 * nsel, 0.0);
+  const int64_t nblk = (M + NB - 1) / NB;
+#pragma omp parallel num_threads(nth)
+  {
+    double* acc = part.data() + size_t(omp_get_thread_num()) * 2 * nsel;
+    std::vector<double> tc[kMaxV], ts[kMaxV];
+    for (int v = 0; v < V.nv; ++v) {
+      tc[v].assign(V.n[v] * NB, 0.0);
+      ts[v].assign(V.n[v] * NB, 0.0);
+    }
+    double hr[NB], hi[NB];
+#pragma omp for schedule(static)
+    for (int64_t b = 0; b < nblk; ++b) {
+      const int64_t j0 = b * NB;
+      const int nb = int(std::min<int64_t>(NB, M - j0));
+      for (int jj = 0; jj < NB; ++jj) {
+        hr[jj] = jj < nb ? fhat[2 * (j0 + jj)] : 0.0;
+        hi[jj] = jj < nb ? fhat[2 * (j0 + jj) + 1] : 0.0;
+      }
+      for (int v = 0; v < V.nv; ++v)
+        for (int jj = 0; jj < NB; ++jj) {
+          const double x = jj < nb ? k[V.dim[v] + int64_t(D) * (j0 + jj)] : 0.0;
+          phase_table(x, 1.0, V.scale[v], V.off[v], V.n[v], tc[v].data() + jj, ts[v].data() + jj, NB);
+        }
+      // fold the node values into the last table: a pair then costs nv - 1 complex products
+      {
+        const int v = V.nv - 1;
+        for (int64_t i = 0; i < V.n[v]; ++i)
+          for (int jj = 0; jj < NB; ++jj) {
+            const double c = tc[v][i * NB + jj], sn = ts[v][i * NB + jj];
+            tc[v][i * NB + jj] = hr[jj] * c - hi[jj] * sn;
+            ts[v][i * NB + jj] = hr[jj] * sn + hi[jj] * c;
+          }
+      }
+      for (int64_t s = 0; s < nsel; ++s) {
+        const int32_t* ix = &vidx[s * V.nv];
+        double pr[NB], pi[NB];
+        {
+          const int v = V.nv - 1;
+          const double* cc = &tc[v][int64_t(ix[v]) * NB];
+          const double* ss = &ts[v][int64_t(ix[v]) * NB];
+          for (int jj = 0; jj < NB; ++jj) {
+            pr[jj] = cc[jj];
+            pi[jj] = ss[jj];
+          }
+        }
+        for (int v = V.nv - 2; v >= 0; --v) {
+          const double* cc = &tc[v][int64_t(ix[v]) * NB];
+          const double* ss = &ts[v][int64_t(ix[v]) * NB];
+          for (int jj = 0; jj < NB; ++jj) {
+            const double t = pr[jj] * cc[jj] - pi[jj] * ss[jj];
+            pi[jj] = pr[jj] * ss[jj] + pi[jj] * cc[jj];
+            pr[jj] = t;
+          }
+        }
+        double sr = 0.0, si = 0.0;
+        for (int jj = 0; jj < NB; ++jj) {
+          sr += pr[jj];
+          si += pi[jj];
+        }
+        acc[2 * s] += sr;
+        acc[2 * s + 1] += si;
+      }
+    }
+  }
+  for (int64_t s = 0; s < nsel; ++s) {
+    double sr = 0.0, si = 0.0;
+    for (int t = 0; t < nth; ++t) {
+      sr += part[size_t(t) * 2 * nsel + 2 * s];
+      si += part[size_t(t) * 2 * nsel + 2 * s + 1];
+    }
+    out[2 * s] = sr;
+    out[2 * s + 1] = si;
   }
 }
 

@@ -73,6 +73,8 @@ def lib():
                 getattr(L, f"oracle_deconvolve_transpose_{suf}").argtypes = [ctypes.c_int, i64p, i64p, dp, dp, dp, dp, dp]
             L.oracle_ndft_forward.argtypes = [ctypes.c_int, i64p, ctypes.c_int64, dp, dp, dp]
             L.oracle_ndft_adjoint.argtypes = [ctypes.c_int, i64p, ctypes.c_int64, dp, dp, ctypes.c_int64, i64p, dp]
+            L.oracle_ndft_adjoint_sel.argtypes = [ctypes.c_int, i64p, ctypes.c_int64, dp, dp, ctypes.c_int64, i64p,
+                                                  dp]
             L.oracle_window_phi.restype = ctypes.c_double
             L.oracle_window_phi.argtypes = [ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_int, ctypes.c_double]
             L.oracle_num_threads.restype = ctypes.c_int
@@ -231,6 +233,21 @@ def chebyshev_interp(fun, a, b, n, x):
     return t * b1 - b2 + c[0]
 
 
+def sort_nodes_lex(k):
+    """k .= sortslices(k, dims=2) (src/precomputation.jl:52-54,
+    src/implementation.jl:112-114): the columns of the D x M node array sorted
+    in place in lexicographic order, dimension 1 first, each coordinate by
+    Julia's isless (-0.0 before 0.0; nodes are checked before, so no NaN).
+    Returns the permutation (new column i = old column perm[i])."""
+    keys = []
+    for d in reversed(range(k.shape[0])):
+        keys.append(~np.signbit(k[d]))  # ties of equal values: -0.0 first
+        keys.append(k[d])
+    perm = np.lexsort(keys)
+    k[...] = k[:, perm]
+    return perm
+
+
 def index_offset(n):
     """indexOffset, src/precomputation.jl:345."""
     return (-1 - n // 2) if n % 2 == 0 else (-1 - (n - 1) // 2)
@@ -258,7 +275,7 @@ class OraclePlan:
     155-193)."""
 
     def __init__(self, k, N, *, m=None, sigma=None, reltol=None, window="kaiser_bessel",
-                 precompute=TENSOR, blockSize=None, dtype=np.float64, fft_workers=None):
+                 precompute=TENSOR, blockSize=None, dtype=np.float64, fft_workers=None, sortNodes=False):
         k = np.asarray(k)
         if k.ndim == 1:
             k = k.reshape(1, -1)
@@ -278,6 +295,12 @@ class OraclePlan:
         kk = np.ascontiguousarray(k.T.astype(self.dtype))  # column-major D x M
         if not np.all(np.abs(kk) <= 0.5):  # checkNodes, src/utils.jl:46-55
             raise ValueError("Nodes k need to be within the range [-1/2, 1/2)")
+        if sortNodes:  # k .= sortslices(k, dims=2) on the caller's array, src/precomputation.jl:52-54
+            kd = np.array(k, dtype=self.dtype)
+            sort_nodes_lex(kd)
+            if k.flags.writeable:
+                k[...] = kd
+            kk = np.ascontiguousarray(kd.T)
         self.k = kk
         self.coeffs = poly_coefficients(window, self.m, self.sigma)
         # polynomial coefficients are stored in T (Matrix{T}, :306)
@@ -398,9 +421,15 @@ def ndft_forward(k, f, subset=None):
     return out
 
 
-def ndft_adjoint(k, N, fhat, subset=None):
+def ndft_adjoint(k, N, fhat, subset=None, method=None):
     """Direct adjoint NDFT, src/direct.jl:126-151, FP64; with ``subset`` (linear
-    column-major indices) only those outputs are returned (flat)."""
+    column-major indices) only those outputs are returned (flat).
+
+    ``method``: "direct" evaluates cos/sin for every (node, output) pair (the
+    default without a subset); "table" builds per-node phase tables of at most
+    256 entries per (virtual) dimension and multiplies their entries (the
+    default with a subset: ~20 flops per pair, used for the full-size NDFT
+    subsets)."""
     k = np.asarray(k, dtype=np.float64)
     if k.ndim == 1:
         k = k.reshape(1, -1)
@@ -412,10 +441,43 @@ def ndft_adjoint(k, N, fhat, subset=None):
     sel_a, sel_p = _i64(sel)
     out = np.zeros(sel.size, np.complex128)
     N_a, N_p = _i64(N)
-    lib().oracle_ndft_adjoint(D, N_p, kk.shape[0], kk.ctypes.data, fh.ctypes.data, sel.size, sel_p, out.ctypes.data)
+    if method is None:
+        method = "direct" if subset is None else "table"
+    fn = lib().oracle_ndft_adjoint if method == "direct" else lib().oracle_ndft_adjoint_sel
+    fn(D, N_p, kk.shape[0], kk.ctypes.data, fh.ctypes.data, sel.size, sel_p, out.ctypes.data)
     if subset is None:
         return out.reshape(N, order="F")
     return out
+
+
+# The NFFT.jl TENSOR series of the paper's accuracy figure at D = 2, N = 512^2,
+# J = |N|, sigma = 2 (benchmark/paper/img/accuracy_m_D2_.tex:40-43 forward,
+# :87-90 adjoint): mean relative l2 error over the script's P = 10 runs.
+PAPER_D2_TENSOR = {
+    "forward": {3: 7.662783919423607e-6, 4: 5.747972034947691e-8, 5: 6.130420281952177e-10,
+                6: 8.923266708493597e-12},
+    "adjoint": {3: 6.932655431859695e-6, 4: 6.318935476675504e-8, 5: 7.001282121332577e-10,
+                6: 7.660093463898552e-12},
+}
+
+
+def paper_d2_runs(nruns=10, seed=1):
+    """The inputs of benchmark/paper/accuracyNew.jl:29-45 at D = 2 (N = 512^2,
+    J = |N|, sigma = 2), run by run: nodes rand(2, J) - 1/2, fHat =
+    randn(ComplexF64, J) (each part N(0, 1/2)), f = rand(ComplexF64, N) (each
+    part U[0, 1)).  Each run yields (k, f, fhat, truth_forward, truth_adjoint),
+    the ground truth from an FP64 FULL-precompute plan at m = 8: the script
+    used NFFT3 at m = 12, and both sit at the ~2e-14 floor of the figure
+    (accuracy_m_D2_.tex:45-47), far below the m <= 6 errors compared."""
+    rng = np.random.default_rng(seed)
+    N = (512, 512)
+    J = N[0] * N[1]
+    for _ in range(nruns):
+        k = rng.random((2, J)) - 0.5
+        fhat = (rng.standard_normal(J) + 1j * rng.standard_normal(J)) / math.sqrt(2)
+        f = rng.random(N) + 1j * rng.random(N)
+        g = OraclePlan(k, N, m=8, sigma=2.0, precompute=FULL)
+        yield k, f, fhat, g.forward(f), g.adjoint(fhat)
 
 
 def rel_l2(x, ref):

@@ -131,14 +131,15 @@ def test_batch_config4_64_plans():
     for i, (p, (k, N)) in enumerate(zip(plans, probs)):
         assert oracle.rel_l2(ys[i].cpu().numpy(), (p * fs[i]).cpu().numpy()) <= 1e-6, i
         assert oracle.rel_l2(xs[i].cpu().numpy(), (nf.adjoint(p) * vs[i]).cpu().numpy()) <= 1e-6, i
-    # accuracy against the FP64 NDFT on node / frequency subsets of a few plans
-    for i in (0, 17, 63):
-        k, N = probs[i]
+    # accuracy of every member against the FP64 NDFT (oracle) on 256 random
+    # nodes (forward) and 256 random output frequencies (adjoint)
+    for i, (k, N) in enumerate(probs):
         k64 = k.astype(np.float64)
         f = fs[i].cpu().numpy().astype(np.complex128)
-        sub = np.random.default_rng(i).choice(k.shape[1], 64, replace=False)
+        rs = np.random.default_rng(100 + i)
+        sub = rs.choice(k.shape[1], 256, replace=False)
+        lin = rs.choice(N[0] * N[1], 256, replace=False)
         ref = oracle.ndft_forward(k64, f, subset=sub)
-        assert oracle.rel_l2(ys[i].cpu().numpy()[sub], ref) < 1e-5, i
-        lin = np.random.default_rng(i + 1).choice(N[0] * N[1], 32, replace=False)
+        assert oracle.rel_l2(ys[i].cpu().numpy()[sub], ref) <= 1e-5, i
         refx = oracle.ndft_adjoint(k64, N, vs[i].cpu().numpy().astype(np.complex128), subset=lin)
-        assert oracle.rel_l2(xs[i].cpu().numpy().ravel(order="F")[lin], refx) < 1e-5, i
+        assert oracle.rel_l2(xs[i].cpu().numpy().ravel(order="F")[lin], refx) <= 1e-5, i

@@ -288,3 +288,31 @@ def test_fused_fft_1024_lines(N, prec):
     tol = TOL64 if prec == 64 else TOL32
     assert oracle.rel_l2(y, op.forward(f)) < tol
     assert oracle.rel_l2(colmajor_flat(x), colmajor_flat(op.adjoint(fhat))) < tol
+
+
+def test_paper_accuracy_d2_tensor_gpu_fp64():
+    """The GPU FP64 TENSOR plan at the paper's configuration (N = 512^2,
+    J = |N|, sigma = 2, m = 3..6, 10 runs; benchmark/paper/accuracyNew.jl,
+    accuracy_m_D2_.tex:40-43 and :87-90): equal to the oracle's plan (1e-11 on
+    the first run) and reproducing both published series within the bands of
+    the oracle's own test (adjoint 1.25x, forward 1.5x: the forward statistic
+    is dominated by the few nodes near k = 0)."""
+    ms = (3, 4, 5, 6)
+    ef = {m: [] for m in ms}
+    ea = {m: [] for m in ms}
+    for run, (k, f, fhat, gf, ga) in enumerate(oracle.paper_d2_runs()):
+        for m in ms:
+            p = nf.plan_nfft(k, f.shape, m=m, sigma=2.0, precompute=nf.TENSOR)
+            y, x = gpu_fwd_adj(p, f, fhat)
+            if run == 0:
+                op = oracle.OraclePlan(k, f.shape, m=m, sigma=2.0, precompute=oracle.TENSOR)
+                assert oracle.rel_l2(y, op.forward(f)) < TOL64, m
+                assert oracle.rel_l2(x, op.adjoint(fhat)) < TOL64, m
+            ef[m].append(oracle.rel_l2(y, gf))
+            ea[m].append(oracle.rel_l2(x, ga))
+            del p
+    for m in ms:
+        rf = np.mean(ef[m]) / oracle.PAPER_D2_TENSOR["forward"][m]
+        ra = np.mean(ea[m]) / oracle.PAPER_D2_TENSOR["adjoint"][m]
+        assert 1 / 1.5 < rf < 1.5, (m, rf)
+        assert 1 / 1.25 < ra < 1.25, (m, ra)

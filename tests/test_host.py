@@ -55,17 +55,20 @@ def test_bench_sparse_b_comparator_matches_oracle(N):
     assert oracle.rel_l2(x, op.adjoint(fh).ravel(order="F")) < 1e-13
 
 
-def test_bench_ndft_checker_matches_oracle():
+def test_bench_error_subsets_and_frequencies():
+    """bench.py's error measurement: 4096 distinct sorted nodes / outputs, and
+    the frequencies n - N div 2 of column-major output indices (the NNDFT
+    points whose adjoint equals the NDFT adjoint there)."""
     import bench
-    from oracle import oracle
-    rng = np.random.default_rng(3)
-    N, M = (6, 8, 10), 40
-    k = rng.random((3, M)) - 0.5
-    f = rng.standard_normal(N) + 1j * rng.standard_normal(N)
-    fh = rng.standard_normal(M) + 1j * rng.standard_normal(M)
-    sub, lin = np.arange(0, M, 3), np.arange(0, 480, 7)
-    assert oracle.rel_l2(bench.ndft_forward_subset(k, f, sub), oracle.ndft_forward(k, f, subset=sub)) < 1e-13
-    assert oracle.rel_l2(bench.ndft_adjoint_subset(k, N, fh, lin), oracle.ndft_adjoint(k, N, fh, subset=lin)) < 1e-13
+    sub, lin = bench.error_subsets(10 ** 6, 256 ** 3)
+    assert len(sub) == len(np.unique(sub)) == 4096 and np.all(np.diff(sub) > 0)
+    assert len(lin) == 4096 and lin.max() < 256 ** 3
+    N = (6, 8, 10)
+    lin = np.arange(0, 480, 7)
+    fr = bench.frequencies(N, lin)
+    grids = np.meshgrid(*[np.arange(n) - n // 2 for n in N], indexing="ij")
+    for d in range(3):
+        assert np.array_equal(fr[d], grids[d].ravel(order="F")[lin])
 
 
 def test_bench_clock_sampler_keeps_the_timed_region():

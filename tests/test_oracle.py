@@ -43,21 +43,38 @@ def test_high_level_fp32():
     assert oracle.rel_l2(p.adjoint(fhat.astype(np.complex64)), f) < 1e-3
 
 
-@pytest.mark.parametrize("m,published", [(3, 7.66e-6), (4, 5.75e-8), (5, 6.13e-10), (6, 8.92e-12)])
-def test_paper_accuracy_band(m, published):
-    """benchmark/paper/img/accuracy_m_D2_.tex:36 -- TENSOR forward rel l2 error
-    at D=2, sigma=2 (published for N=512^2); a 2-D 96^2 case must land within
-    a factor 3 of the published value."""
-    rng = np.random.default_rng(11)
-    N = (96, 96)
-    J = int(np.prod(N))
-    k = rng.random((2, J)) - 0.5
-    f = rng.random(N) + 1j * rng.random(N)
-    sub = rng.choice(J, 400, replace=False)
-    g = oracle.ndft_forward(k, f, subset=sub)
-    p = oracle.OraclePlan(k, N, m=m, sigma=2.0, precompute=oracle.TENSOR)
-    e = oracle.rel_l2(p.forward(f)[sub], g)
-    assert published / 3 < e < published * 3
+def test_paper_accuracy_d2_tensor():
+    """The published accuracy of NFFT.jl's TENSOR plan at the paper's own
+    configuration (benchmark/paper/accuracyNew.jl:15-59: D = 2, N = 512^2,
+    J = |N|, sigma = 2, P = 10 runs; accuracy_m_D2_.tex:40-43 forward, :87-90
+    adjoint), m = 3..6: the mean relative l2 error over 10 runs of the oracle
+    must reproduce both published series.
+
+    The adjoint statistic is stable (run-to-run spread ~1 %) and must land
+    within 1.25x.  The forward input f = rand(ComplexF64, N) has mean (1+i)/2,
+    so |A f| is dominated by the few nodes within 1/N of k = 0 and the
+    per-run relative error spreads by ~35 %; the 10-run means (the paper's
+    and this one) must agree within 1.5x.  The ground truth (FULL plan, m = 8)
+    is itself checked against the FP64 NDFT on 4096 nodes / frequencies."""
+    ms = (3, 4, 5, 6)
+    ef = {m: [] for m in ms}
+    ea = {m: [] for m in ms}
+    for run, (k, f, fhat, gf, ga) in enumerate(oracle.paper_d2_runs()):
+        if run == 0:
+            rng = np.random.default_rng(5)
+            sub = np.sort(rng.choice(k.shape[1], 4096, replace=False))
+            lin = np.sort(rng.choice(f.size, 4096, replace=False))
+            assert oracle.rel_l2(gf[sub], oracle.ndft_forward(k, f, subset=sub)) < 1e-12
+            assert oracle.rel_l2(ga.ravel(order="F")[lin], oracle.ndft_adjoint(k, f.shape, fhat, subset=lin)) < 1e-12
+        for m in ms:
+            p = oracle.OraclePlan(k, f.shape, m=m, sigma=2.0, precompute=oracle.TENSOR)
+            ef[m].append(oracle.rel_l2(p.forward(f), gf))
+            ea[m].append(oracle.rel_l2(p.adjoint(fhat), ga))
+    for m in ms:
+        rf = np.mean(ef[m]) / oracle.PAPER_D2_TENSOR["forward"][m]
+        ra = np.mean(ea[m]) / oracle.PAPER_D2_TENSOR["adjoint"][m]
+        assert 1 / 1.5 < rf < 1.5, (m, rf)
+        assert 1 / 1.25 < ra < 1.25, (m, ra)
 
 
 @pytest.mark.parametrize("pre", [oracle.LINEAR, oracle.FULL, oracle.TENSOR, oracle.POLYNOMIAL])
