@@ -83,8 +83,11 @@ typedef struct {
   int32_t precompute;       /* NFFT_PRECOMPUTE_* */
   int32_t blocking;         /* 1: bin-sorted tiled kernels; 0: per-node kernels
                                with global atomics (the plain path) */
-  int32_t sort_nodes;       /* accepted for interface parity; nodes are always
-                               binned on the device when blocking = 1 */
+  int32_t sort_nodes;       /* sortNodes: 1 = the host binding sorts the caller's
+                               k in place with nfft_sort_nodes before
+                               nfft_set_nodes (the reference's in-place
+                               sortslices); nfft_set_nodes itself never
+                               reorders k */
   int32_t store_deconv_idx; /* accepted for interface parity; deconvolution is
                                fused with padding/cropping */
   int64_t block_size[3];    /* tile (block) size per dimension; 0 = automatic */
@@ -141,6 +144,16 @@ int nfft_set_stream(nfft_plan* plan, void* stream);
  * and builds the spreading task list.  k is D x M of the plan's real type;
  * k_on_device selects a device or a host pointer.  Synchronises the stream. */
 int nfft_set_nodes(nfft_plan* plan, const void* k, int k_on_device);
+
+/* k .= sortslices(k, dims=2), the sortNodes = true step of plan_nfft and
+ * nodes! (src/precomputation.jl:52-54, src/implementation.jl:112-114):
+ * sorts the columns of the D x M node array k (precision 32 or 64) in place
+ * in lexicographic order (dimension 1 first; isless per coordinate, -0.0
+ * before 0.0) with a stable device radix sort.  k is a device or a host
+ * pointer (k_on_device).  The nodes are checked like checkNodes first
+ * (src/utils.jl:46-55): invalid nodes return NFFT_ERR_NODE_OUT_OF_RANGE and
+ * leave k untouched.  Synchronous on stream (NULL: legacy default stream). */
+int nfft_sort_nodes(int precision, int D, int64_t M, void* k, int k_on_device, void* stream);
 
 /* mul!(fHat, p, f) (src/implementation.jl:155-172,
  * ext/NFFTGPUArraysExt/implementation.jl:97-115): fused pad + apodize,

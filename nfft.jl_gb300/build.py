@@ -22,7 +22,8 @@ OUT = os.path.join(HERE, "nfftgb300", "libnfftgb300.so")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 
 SOURCES = ["plan.cu", "precompute.cu", "sort.cu", "deconv.cu", "interp.cu", "spread.cu", "gradk.cu", "batch.cu",
-           "directional.cu", "fft.cu", "plain.cu", "noalloc.cu", "autotune.cu", "toeplitz.cu", "direct.cu", "trig.cu", "nnfft.cu"]
+           "directional.cu", "fft.cu", "plain.cu", "noalloc.cu", "autotune.cu", "toeplitz.cu", "direct.cu", "trig.cu", "nnfft.cu",
+           "sortnodes.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

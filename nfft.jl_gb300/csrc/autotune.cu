@@ -23,6 +23,7 @@ namespace {
 std::mutex g_cache_mutex;
 std::map<std::string, std::vector<int64_t>> g_cache;
 bool g_cache_loaded = false;
+std::string g_cache_path;  // the NFFT_GB300_TUNE_CACHE value the cache was read from
 
 std::string cache_key(const nfft_plan* p) {
   int dev = 0, sms = 0;
@@ -37,11 +38,16 @@ std::string cache_key(const nfft_plan* p) {
   return buf;
 }
 
-// Cache file: one line per entry, "key bs0 bs1 bs2 ny".
+// Cache file: one line per entry, "key bs0 bs1 bs2 ny".  Read once per value
+// of NFFT_GB300_TUNE_CACHE: pointing the variable at another file (re)loads
+// from that file.
 void load_cache() {
-  if (g_cache_loaded) return;
-  g_cache_loaded = true;
   const char* path = getenv("NFFT_GB300_TUNE_CACHE");
+  const std::string cur = path ? path : "";
+  if (g_cache_loaded && cur == g_cache_path) return;
+  g_cache_loaded = true;
+  g_cache_path = cur;
+  g_cache.clear();
   if (!path) return;
   FILE* f = fopen(path, "r");
   if (!f) return;
@@ -115,9 +121,14 @@ int apply_block_size(nfft_plan* p, const int64_t* bs, const void* k, int ny) {
     p->prm.block_size[d] = d < p->D ? nb[d] : 0;
   }
   p->ntiles_total = nt;
-  p->spread_ny = (p->D == 3 && !p->prm.compensated && ny == 2) ? 2 : 1;
+  p->spread_layout = (p->D == 3 && !p->prm.compensated && (ny == 2 || ny == 3)) ? ny : 1;
+  if (p->spread_layout == 3 && !spread_cols_supported(p)) {
+    set_error("spreading layout 3 needs FP32, D = 3, uncompensated tiles with blockSize[3] of 8 or 16 and at most "
+              "24 warps of 8 x 4 columns");
+    return NFFT_ERR_UNSUPPORTED;
+  }
   p->spread_pitch = spread_pitch_for(p->D, p->m, int(p->bs[0]) + 2 * p->m - 1,
-                                     int((p->prm.compensated ? 4 : 2) * p->real_size), p->spread_ny);
+                                     int((p->prm.compensated ? 4 : 2) * p->real_size), p->spread_layout == 2 ? 2 : 1);
   p->gather_pitch = spread_pitch_for(p->D == 2 ? 3 : p->D, p->m, int(p->bs[0]) + 2 * p->m - 1,
                                      int(2 * p->real_size), 1);
   return nfft_set_nodes(p, k, 1);
@@ -164,7 +175,7 @@ extern "C" int nfft_autotune(nfft_plan* p, int use_cache) {
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
   double best = 1e30;
-  std::vector<int64_t> best_bs = {p->bs[0], p->bs[1], p->bs[2], p->spread_ny};
+  std::vector<int64_t> best_bs = {p->bs[0], p->bs[1], p->bs[2], p->spread_layout};
   for (const auto& c : candidates(p)) {
     if (apply_block_size(p, c.data(), k, int(c[3])) != NFFT_OK) continue;
     float times[3];
@@ -199,7 +210,7 @@ extern "C" int nfft_autotune(nfft_plan* p, int use_cache) {
 extern "C" int nfft_set_tiling(nfft_plan* p, const int64_t* block_size, int row_parity_warps);
 
 extern "C" int nfft_set_block_size(nfft_plan* p, const int64_t* block_size) {
-  return nfft_set_tiling(p, block_size, p ? p->spread_ny : 1);
+  return nfft_set_tiling(p, block_size, p ? p->spread_layout : 1);
 }
 
 extern "C" int nfft_set_tiling(nfft_plan* p, const int64_t* block_size, int row_parity_warps) {
@@ -212,8 +223,8 @@ extern "C" int nfft_set_tiling(nfft_plan* p, const int64_t* block_size, int row_
       set_error("block size must be positive");
       return NFFT_ERR_INVALID_ARG;
     }
-  if (row_parity_warps != 1 && row_parity_warps != 2) {
-    set_error("row_parity_warps must be 1 or 2");
+  if (row_parity_warps < 1 || row_parity_warps > 3) {
+    set_error("the spreading layout must be 1, 2 or 3");
     return NFFT_ERR_INVALID_ARG;
   }
   if (!p->has_nodes) {

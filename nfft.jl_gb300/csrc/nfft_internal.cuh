@@ -130,7 +130,8 @@ struct nfft_plan {
   int64_t n_tasks = 0;
   int4* tasks = nullptr;
   int spread_pitch = 0;            // shared-memory row pitch of the padded spreading tile
-  int spread_ny = 1;               // D = 3: 2 = 16-warp tiles owning (slice group, row parity)
+  int spread_layout = 1;           // D = 3 spreading kernel: 1 = 8 warps owning slices, 2 = 16 warps owning
+                                   // (slice group, row parity), 3 = register columns (FP32, spread_cols.cuh)
   int gather_pitch = 0;            // shared-memory row pitch of the staged gather tile
   bool gather_tiled = false;       // gather from shared-memory tiles (else straight from L1/L2)
   int* dflag = nullptr;            // device status word
@@ -154,6 +155,8 @@ namespace nfft {
 // ------------------------------------------------------------------ launchers
 // precompute.cu
 int launch_check_nodes(const nfft_plan* p, const void* k, int* flag);
+// the same check on n values of the given precision, without a plan
+int launch_check_node_values(int precision, const void* k, int64_t n, int* flag, cudaStream_t s);
 int launch_reduce_nodes(const nfft_plan* p, const void* k, int32_t* ti_u, void* te_u, uint32_t* key,
                         int32_t* val, int32_t* tile_count);
 int launch_build_node_tables(const nfft_plan* p, const int32_t* perm, const int32_t* ti_u, const void* te_u);
@@ -164,6 +167,8 @@ int launch_build_tasks(nfft_plan* p, int chunk);
 int apply_block_size(nfft_plan* p, const int64_t* bs, const void* k, int ny);
 // spread.cu: bank-conflict-free row pitch of a padded spreading tile
 int spread_pitch_for(int D, int m, int P0, int elem_bytes, int ny);
+// spread.cu: whether spreading layout 3 (register columns) runs this plan's tiles
+bool spread_cols_supported(const nfft_plan* p);
 // sort.cu
 int radix_sort_pairs(uint32_t* keys, int32_t* vals, uint32_t* keys_tmp, int32_t* vals_tmp, int64_t n,
                      int key_bits, void* scratch, size_t scratch_bytes, cudaStream_t s,

@@ -12,6 +12,7 @@
 #include "nfft_internal.cuh"
 
 #include <algorithm>
+#include <map>
 #include <mutex>
 
 namespace {
@@ -23,31 +24,64 @@ constexpr size_t kScratchBytes = size_t(16) << 20;  // 16 MiB
 
 static __device__ __align__(256) unsigned char g_bin_scratch[kScratchBytes];
 
-constexpr int kMaxDevices = 64;
 std::mutex g_setup_mutex;
-void* g_scratch_ptr[kMaxDevices] = {};
+// device address of g_bin_scratch per CUDA context (by the driver's unique
+// context id, so a context that was reset and re-created is looked up anew)
+std::map<unsigned long long, void*> g_scratch_ptr;
 
-// Device address of g_bin_scratch on the current device.  In host code the
-// symbol is only a host-side stand-in, so the address is looked up once per
-// device with that device current, on the first call made there.
-int scratch_for_current_device(void** out) {
-  int dev = 0;
-  NFFT_CUDA_TRY(cudaGetDevice(&dev));
-  if (dev < 0 || dev >= kMaxDevices) {
-    nfft::set_error("device ordinal %d out of range", dev);
-    return NFFT_ERR_INVALID_ARG;
-  }
-  std::lock_guard<std::mutex> lock(g_setup_mutex);
-  if (!g_scratch_ptr[dev]) {
-    void* ptr = nullptr;
-    cudaError_t err = cudaGetSymbolAddress(&ptr, g_bin_scratch);
-    if (err != cudaSuccess || !ptr) {
-      nfft::set_error("cudaGetSymbolAddress of the binning scratch failed: %s", cudaGetErrorString(err));
-      return NFFT_ERR_CUDA;
+using CtxGetCurrentFn = int (*)(void**);
+using CtxGetIdFn = int (*)(void*, unsigned long long*);
+
+// Unique id of the calling thread's current context, 0 if the driver does not
+// provide one.  The driver entry points are resolved through the runtime, so
+// the library does not link the driver library itself.
+unsigned long long current_context_id() {
+  static CtxGetCurrentFn get_current = nullptr;
+  static CtxGetIdFn get_id = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* a = nullptr;
+    void* b = nullptr;
+    cudaDriverEntryPointQueryResult qa{}, qb{};
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &a, 12000, cudaEnableDefault, &qa) == cudaSuccess &&
+        qa == cudaDriverEntryPointSuccess && a &&
+        cudaGetDriverEntryPointByVersion("cuCtxGetId", &b, 12000, cudaEnableDefault, &qb) == cudaSuccess &&
+        qb == cudaDriverEntryPointSuccess && b) {
+      get_current = reinterpret_cast<CtxGetCurrentFn>(a);
+      get_id = reinterpret_cast<CtxGetIdFn>(b);
     }
-    g_scratch_ptr[dev] = ptr;
+  });
+  void* ctx = nullptr;
+  unsigned long long id = 0;
+  if (get_current && get_id && get_current(&ctx) == 0 && ctx && get_id(ctx, &id) == 0) return id;
+  return 0;
+}
+
+// Device address of g_bin_scratch in the current device's context.  In host
+// code the symbol is only a host-side stand-in, so the address is looked up
+// with cudaGetSymbolAddress, with that device current, on the first call made
+// in each context (which also loads the module there; this first call should
+// come before any stream capture).  Without a context id the lookup is
+// repeated on every call.
+int scratch_for_current_device(void** out) {
+  unsigned long long ctx = current_context_id();  // 0 before the runtime made a context current
+  std::lock_guard<std::mutex> lock(g_setup_mutex);
+  if (ctx) {
+    auto it = g_scratch_ptr.find(ctx);
+    if (it != g_scratch_ptr.end()) {
+      *out = it->second;
+      return NFFT_OK;
+    }
   }
-  *out = g_scratch_ptr[dev];
+  void* ptr = nullptr;
+  cudaError_t err = cudaGetSymbolAddress(&ptr, g_bin_scratch);
+  if (err != cudaSuccess || !ptr) {
+    nfft::set_error("cudaGetSymbolAddress of the binning scratch failed: %s", cudaGetErrorString(err));
+    return NFFT_ERR_CUDA;
+  }
+  if (!ctx) ctx = current_context_id();  // the lookup initialised the device's primary context
+  if (ctx) g_scratch_ptr[ctx] = ptr;
+  *out = ptr;
   return NFFT_OK;
 }
 

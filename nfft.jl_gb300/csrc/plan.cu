@@ -151,8 +151,12 @@ void default_block(nfft_plan* p) {
     p->bs[d] = b;
   }
   // small grids: halve the largest tile side (down to 8) until there are at
-  // least 4 tiles per SM of a GB300 (152 SMs), so the spreading tasks fill it
+  // least 4 tiles per SM of the plan's GPU, so the spreading tasks fill it
   if (!user) {
+    int dev = 0, sms = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) !=
+                                                  cudaSuccess || sms < 1)
+      sms = 1;
     for (;;) {
       int64_t nt = 1;
       int dmax = 0;
@@ -160,7 +164,7 @@ void default_block(nfft_plan* p) {
         nt *= (p->Nt[d] + p->bs[d] - 1) / p->bs[d];
         if (p->bs[d] > p->bs[dmax]) dmax = d;
       }
-      if (nt >= 4 * 152 || p->bs[dmax] <= 8) break;
+      if (nt >= 4 * int64_t(sms) || p->bs[dmax] <= 8) break;
       p->bs[dmax] /= 2;
     }
   }
@@ -468,7 +472,7 @@ int nfft_plan_create(nfft_plan** out, int precision, int D, const int64_t* N, in
   p->lut_size = lut_size_for(p->m);
   default_block(p);
   p->spread_pitch = spread_pitch_for(D, p->m, int(p->bs[0]) + 2 * p->m - 1,
-                                     int((prm.compensated ? 4 : 2) * (precision == 32 ? 4 : 8)), p->spread_ny);
+                                     int((prm.compensated ? 4 : 2) * (precision == 32 ? 4 : 8)), 1);
   p->gather_pitch = spread_pitch_for(D == 2 ? 3 : D, p->m, int(p->bs[0]) + 2 * p->m - 1,
                                      int(2 * (precision == 32 ? 4 : 8)), 1);
   if (const char* e = getenv("NFFT_GB300_GATHER_TILED")) p->gather_tiled = e[0] == '1';
@@ -689,7 +693,7 @@ int nfft_plan_copy(const nfft_plan* src, nfft_plan** out) {
   if (!src || !out) return NFFT_ERR_INVALID_ARG;
   int rc = nfft_plan_create(out, src->precision, src->D, src->N, src->M, &src->prm, src->stream);
   if (rc) return rc;
-  (*out)->spread_ny = src->spread_ny;  // same tile shape (prm.block_size), same warp layout
+  (*out)->spread_layout = src->spread_layout;  // same tile shape (prm.block_size), same warp layout
   (*out)->spread_pitch = src->spread_pitch;
   if (src->has_nodes) {
     rc = nfft_set_nodes(*out, src->k, 1);

@@ -166,6 +166,16 @@ int launch_check_nodes(const nfft_plan* p, const void* k, int* flag) {
   return p->precision == 32 ? check_nodes_t<float>(p, k, flag) : check_nodes_t<double>(p, k, flag);
 }
 
+int launch_check_node_values(int precision, const void* k, int64_t n, int* flag, cudaStream_t s) {
+  if (n == 0) return NFFT_OK;
+  if (precision == 32)
+    check_nodes_kernel<float><<<unsigned((n + 255) / 256), 256, 0, s>>>(static_cast<const float*>(k), n, flag);
+  else
+    check_nodes_kernel<double><<<unsigned((n + 255) / 256), 256, 0, s>>>(static_cast<const double*>(k), n, flag);
+  NFFT_LAUNCH_CHECK();
+  return NFFT_OK;
+}
+
 template <typename T>
 static int reduce_t(const nfft_plan* p, const void* k, int32_t* ti_u, void* te_u, uint32_t* key, int32_t* val,
                     int32_t* tile_count) {

@@ -20,7 +20,7 @@ using AbstractNFFTs
 using LinearAlgebra
 using CUDA
 
-const libnfft = Ref{String}(joinpath(@__DIR__, "..", "nfftgb300", "libnfftgb300.so"))
+const libnfft = Ref{String}(joinpath(@__DIR__, "..", "..", "nfftgb300", "libnfftgb300.so"))
 
 # ---------------------------------------------------------------- C structs
 
@@ -146,9 +146,19 @@ function bind_stream!(p::GB300NFFTPlan)
   check(ccall((:nfft_set_stream, libnfft[]), Cint, (Ptr{Cvoid}, Ptr{Cvoid}), p.handle, CUDA.stream().handle))
 end
 
+# k .= sortslices(k, dims=2) on the caller's array (sortNodes = true,
+# src/precomputation.jl:52-54, src/implementation.jl:112-114), sorted on the
+# device by nfft_sort_nodes after the checkNodes test.
+function sort_nodes!(k::Matrix{T}) where {T<:Union{Float32,Float64}}
+  check(ccall((:nfft_sort_nodes, libnfft[]), Cint, (Cint, Cint, Int64, Ptr{T}, Cint, Ptr{Cvoid}),
+              T == Float32 ? 32 : 64, size(k, 1), size(k, 2), k, 0, CUDA.stream().handle))
+  return k
+end
+
 function AbstractNFFTs.nodes!(p::GB300NFFTPlan{T}, k::Matrix{T}) where {T}
   size(k, 2) == p.J || throw(DimensionMismatch("nodes! keeps the number of nodes; build a new plan for J ≠ $(p.J)"))
   bind_stream!(p)
+  p.params.sortNodes && sort_nodes!(k)
   check(ccall((:nfft_set_nodes, libnfft[]), Cint, (Ptr{Cvoid}, Ptr{T}, Cint), p.handle, k, 0))
   p.k = k
   return p
@@ -242,7 +252,22 @@ end
 
 function Base.copy(p::GB300NFFTPlan{T,D}) where {T,D}
   AbstractNFFTs.plan_nfft(GB300Backend(), CuArray, copy(p.k), p.N; m=p.params.m, σ=p.params.σ,
-                          window=p.params.window, precompute=p.params.precompute, blocking=p.params.blocking)
+                          window=p.params.window, precompute=p.params.precompute, blocking=p.params.blocking,
+                          sortNodes=p.params.sortNodes)
+end
+
+# nfft(k, f) / nfft_adjoint(k, N, fHat) on device arrays with this backend
+# active (AbstractNFFTs/src/derived.jl:140-151 builds an Array plan; a CuArray
+# argument gets a GPU plan here).  The ChainRulesCore extension
+# (ext/NFFTGB300ChainRulesCoreExt.jl) differentiates both in x and in k.
+function AbstractNFFTs.nfft(b::GB300Backend, k, f::CuArray{Complex{T},D}; kwargs...) where {T,D}
+  p = AbstractNFFTs.plan_nfft(b, CuArray, Matrix{T}(k), size(f); kwargs...)
+  return p * f
+end
+
+function AbstractNFFTs.nfft_adjoint(b::GB300Backend, k, N, fHat::CuVector{Complex{T}}; kwargs...) where {T}
+  p = AbstractNFFTs.plan_nfft(b, CuArray, Matrix{T}(k), Tuple(N); kwargs...)
+  return adjoint(p) * fHat
 end
 
 """

@@ -72,6 +72,7 @@ SIGNATURES = {
     "nfft_plan_copy": (_I, [_P, ctypes.POINTER(_P)]),
     "nfft_set_stream": (_I, [_P, _P]),
     "nfft_set_nodes": (_I, [_P, _P, _I]),
+    "nfft_sort_nodes": (_I, [_I, _I, _I64, _P, _I, _P]),
     "nfft_forward": (_I, [_P, _P, _P]),
     "nfft_adjoint": (_I, [_P, _P, _P]),
     "nfft_convolve": (_I, [_P, _P, _I, _P, _I]),

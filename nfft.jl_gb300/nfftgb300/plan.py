@@ -335,14 +335,25 @@ class GB300NFFTPlan:
             self._create(kk.shape[1])
         lib = L.load()
         self._sync_stream()
+        D, M = kk.shape
         if isinstance(kk, torch.Tensor):
             kt = kk.to(device=self.device, dtype=self.dtype).t().contiguous()  # column-major D x M
+            if self.params.sortNodes:
+                # k .= sortslices(k, dims=2): the caller's tensor is sorted in place
+                _check(lib.nfft_sort_nodes(self.precision, D, M, _ptr(kt), 1, ctypes.c_void_p(self._stream)))
+                kk.copy_(kt.t())
             rc = lib.nfft_set_nodes(self._handle, _ptr(kt), 1)
             self.k = kk
         else:
             kc = np.ascontiguousarray(kk.T.astype(np.float32 if self.precision == 32 else np.float64))
+            if self.params.sortNodes:
+                # k .= sortslices(k, dims=2): the caller's array is sorted in place
+                _check(lib.nfft_sort_nodes(self.precision, D, M, ctypes.c_void_p(kc.ctypes.data), 0,
+                                           ctypes.c_void_p(self._stream)))
+                if kk.flags.writeable:
+                    kk[...] = kc.T
             rc = lib.nfft_set_nodes(self._handle, ctypes.c_void_p(kc.ctypes.data), 0)
-            self.k = np.asarray(kk, dtype=kc.dtype)
+            self.k = np.asarray(kk, dtype=kc.dtype) if not self.params.sortNodes else np.ascontiguousarray(kc.T)
         _check(rc)
         self._timing_update()
         return self
@@ -356,6 +367,7 @@ class GB300NFFTPlan:
         """copy(p): an independent plan with the same nodes."""
         return GB300NFFTPlan(self.k, self.N, m=self.params.m, sigma=self.params.sigma, window=self.params.window,
                              precompute=self.params.precompute, blocking=self.params.blocking,
+                             sortNodes=self.params.sortNodes,
                              blockSize=self.params.blockSize, compensated=self.params.compensated,
                              timing=self._timing, device=self.device)
 

@@ -72,13 +72,32 @@ def test_julia_backend_binds_the_interface_entry_points():
     """The Julia ccall backend (not executable here: no Julia) binds every
     entry point the AbstractNFFTs interface, directional plans and batches
     need; the remaining header functions are inspection / tuning helpers."""
-    jl = open(os.path.join(ROOT, "nfft.jl_gb300", "julia", "NFFTGB300.jl")).read()
+    jl = open(os.path.join(ROOT, "nfft.jl_gb300", "julia", "src", "NFFTGB300.jl")).read()
     helpers = {"nfft_bin_nodes_noalloc", "nfft_get_binning", "nfft_get_deconv_factors", "nfft_get_timing_totals",
                "nfft_kernel_launch_count", "nfft_params_default", "nfft_plan_copy", "nfft_set_block_size",
                "nfft_sync", "nfft_timing_reset"}
     for n in declared_functions():
         if n not in helpers:
             assert f":{n}" in jl, n
+
+
+def test_julia_chainrules_extension():
+    """The Julia backend's ChainRulesCore extension (not executable here: no
+    Julia) is declared in Project.toml and defines the rrules of nfft and
+    nfft_adjoint (AbstractNFFTs/ext/AbstractNFFTsChainRulesCoreExt.jl:31-61)
+    with a node tangent from the library's node-gradient kernel instead of
+    NoTangent."""
+    jdir = os.path.join(ROOT, "nfft.jl_gb300", "julia")
+    proj = open(os.path.join(jdir, "Project.toml")).read()
+    assert "ChainRulesCore" in proj and 'NFFTGB300ChainRulesCoreExt = "ChainRulesCore"' in proj
+    ext = open(os.path.join(jdir, "ext", "NFFTGB300ChainRulesCoreExt.jl")).read()
+    assert "ChainRulesCore.rrule(::typeof(AbstractNFFTs.nfft), k::AbstractMatrix" in ext
+    assert "ChainRulesCore.rrule(::typeof(AbstractNFFTs.nfft_adjoint), k::AbstractMatrix" in ext
+    assert ext.count("NFFTGB300.grad_nodes!(dk, p,") == 2
+    # the node tangent is projected, not NoTangent, in both pullbacks
+    assert ext.count("project_k(Array(dk))") == 2
+    src = open(os.path.join(jdir, "src", "NFFTGB300.jl")).read()
+    assert "function grad_nodes!(" in src and ":nfft_grad_nodes" in src
 
 
 def test_build_compiles_every_source():

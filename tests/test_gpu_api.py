@@ -385,3 +385,85 @@ def test_config5_spiral_gradients_full_size():
     r = q * f64 - y64
     ref = (2 * (nf.adjoint(q) * r)).cpu().numpy()
     assert oracle.rel_l2(fd.grad.cpu().numpy().astype(np.complex128), ref) < 1e-4
+
+
+# ------------------------------------------------------------ sortNodes
+
+def lex_reference(k):
+    """Column order of sortslices(k, dims=2) by a plain stable sort on
+    per-column keys (value, then -0.0 before 0.0, per coordinate)."""
+    M = k.shape[1]
+    return sorted(range(M), key=lambda j: tuple(v for d in range(k.shape[0])
+                                                 for v in (k[d, j], 0 if np.signbit(k[d, j]) else 1)))
+
+
+@pytest.mark.parametrize("D", [1, 2, 3])
+@pytest.mark.parametrize("dtype", [np.float32, np.float64])
+@pytest.mark.parametrize("on_device", [0, 1])
+def test_sort_nodes_matches_sortslices(D, dtype, on_device):
+    """nfft_sort_nodes (host and device arrays) equals sortslices(k, dims=2)
+    bit for bit, ties and signed zeros included."""
+    import ctypes
+    rng = np.random.default_rng(D)
+    M = 3000
+    k = (rng.integers(-6, 6, size=(D, M)) / 12.0).astype(dtype)  # many ties per coordinate
+    k[:, :40] = 0.0
+    k[0, 5:25] = -0.0
+    ref = k[:, lex_reference(k)]
+    k2 = k.copy()
+    assert np.array_equal(k2[:, oracle.sort_nodes_lex(k2.copy())], ref)
+    oracle.sort_nodes_lex(k2)
+    assert np.array_equal(k2, ref) and np.array_equal(np.signbit(k2), np.signbit(ref))
+    lib = nf.load()
+    prec = 32 if dtype == np.float32 else 64
+    if on_device:
+        kt = torch.as_tensor(k.T.copy()).cuda()  # column-major D x M
+        rc = lib.nfft_sort_nodes(prec, D, M, ctypes.c_void_p(kt.data_ptr()), 1, None)
+        out = kt.cpu().numpy().T
+    else:
+        kc = np.ascontiguousarray(k.T)
+        rc = lib.nfft_sort_nodes(prec, D, M, ctypes.c_void_p(kc.ctypes.data), 1 if on_device else 0, None)
+        out = kc.T
+    assert rc == 0
+    assert np.array_equal(out, ref) and np.array_equal(np.signbit(out), np.signbit(ref))
+
+
+@pytest.mark.parametrize("as_tensor", [False, True])
+def test_sort_nodes_plan_matches_oracle(as_tensor):
+    """plan_nfft(k, N; sortNodes=true) sorts the caller's k in place
+    (src/precomputation.jl:52-54) and every output follows that order: fHat
+    equals the oracle's sortNodes plan at 1e-11 (FP64); nodes! sorts too
+    (src/implementation.jl:112-114)."""
+    N = (16, 12, 10)
+    k0 = rand_k(3, 2500, seed=11)
+    k0[:, 100:140] = k0[:, 0:1]  # duplicate nodes
+    f = cnormal(N, 2)
+    fh = cnormal(2500, 3)
+    ref_k = k0[:, lex_reference(k0)]
+    kc = k0.copy()
+    op = oracle.OraclePlan(kc, N, m=4, sigma=2.0, precompute=oracle.TENSOR, sortNodes=True)
+    assert np.array_equal(kc, ref_k)
+    kin = torch.as_tensor(k0.copy()) if as_tensor else k0.copy()
+    p = nf.plan_nfft(kin, N, m=4, sigma=2.0, precompute=nf.TENSOR, sortNodes=True)
+    kin_np = kin.numpy() if as_tensor else kin
+    assert np.array_equal(kin_np, ref_k)
+    y = (p * nf.as_colmajor(f, N, torch.complex128)).cpu().numpy()
+    assert oracle.rel_l2(y, op.forward(f)) < 1e-11
+    x = (nf.adjoint(p) * torch.as_tensor(fh)).cpu().numpy()
+    assert oracle.rel_l2(x, op.adjoint(fh)) < 1e-11
+    # the outputs follow the sorted order: node i of the plan is column i of ref_k
+    y_unsorted = (nf.plan_nfft(k0.copy(), N, m=4, sigma=2.0, precompute=nf.TENSOR) *
+                  nf.as_colmajor(f, N, torch.complex128)).cpu().numpy()
+    assert oracle.rel_l2(y, y_unsorted[lex_reference(k0)]) < 1e-13
+    # nodes!(p, k2) sorts k2 in place as well
+    k2 = rand_k(3, 2500, seed=12)
+    ref2 = k2[:, lex_reference(k2)]
+    p.nodes_(k2)
+    assert np.array_equal(k2, ref2)
+    # invalid nodes: rejected before anything is reordered
+    bad = rand_k(3, 50, seed=13)
+    bad[1, 7] = 0.75
+    keep = bad.copy()
+    with pytest.raises(nf.ArgumentError):
+        nf.plan_nfft(bad, N, m=4, sigma=2.0, sortNodes=True)
+    assert np.array_equal(bad, keep)

@@ -54,6 +54,25 @@ def test_noalloc_binning_matches_set_nodes_twice(dtype):
         assert np.array_equal(tstart, ref["tile_start"])
 
 
+@pytest.mark.parametrize("D,N,bs,M,dtype", [
+    # the static scratch at its limits: 2^18 FP64 nodes in 3-D and exactly 2^18 tiles
+    (3, (64, 64, 64), (2, 2, 2), 1 << 18, np.float64),
+    (1, (1 << 15,), (64,), 50000, np.float32),
+    (2, (128, 100), (16, 8), 70000, np.float64),
+])
+def test_noalloc_binning_at_the_limits_and_in_1d_2d(D, N, bs, M, dtype):
+    rng = np.random.default_rng(D)
+    k = (rng.random((D, M)) - 0.5).astype(dtype)
+    k[:, :3] = np.array([-0.5, 0.5, 0.0], dtype)  # boundary nodes in every dimension
+    p = nf.plan_nfft(k, N, m=4, sigma=2.0, blockSize=bs)
+    ref = p.binning()
+    if D == 3:
+        assert len(ref["tile_start"]) == (1 << 18) + 1
+    perm, tstart = _bin_noalloc(k, p.Ñ, p.params.blockSize)
+    assert np.array_equal(perm, ref["perm"])
+    assert np.array_equal(tstart, ref["tile_start"])
+
+
 def test_noalloc_rejects_oversized_request():
     lib = nf.load()
     Nt = (ctypes.c_int64 * 3)(64, 64, 64)
