@@ -115,18 +115,14 @@ int apply_block_size(nfft_plan* p, const int64_t* bs, const void* k, int ny) {
     set_error("too many tiles");
     return NFFT_ERR_UNSUPPORTED;
   }
+  const int layout = (p->D == 3 && !p->prm.compensated && ny == 2) ? 2 : 1;
   for (int d = 0; d < 3; ++d) {
     p->bs[d] = nb[d];
     p->ntiles[d] = tiles[d];
     p->prm.block_size[d] = d < p->D ? nb[d] : 0;
   }
   p->ntiles_total = nt;
-  p->spread_layout = (p->D == 3 && !p->prm.compensated && (ny == 2 || ny == 3)) ? ny : 1;
-  if (p->spread_layout == 3 && !spread_cols_supported(p)) {
-    set_error("spreading layout 3 needs FP32, D = 3, uncompensated tiles with blockSize[3] of 8 or 16 and at most "
-              "24 warps of 8 x 4 columns");
-    return NFFT_ERR_UNSUPPORTED;
-  }
+  p->spread_layout = layout;
   p->spread_pitch = spread_pitch_for(p->D, p->m, int(p->bs[0]) + 2 * p->m - 1,
                                      int((p->prm.compensated ? 4 : 2) * p->real_size), p->spread_layout == 2 ? 2 : 1);
   p->gather_pitch = spread_pitch_for(p->D == 2 ? 3 : p->D, p->m, int(p->bs[0]) + 2 * p->m - 1,
@@ -223,8 +219,8 @@ extern "C" int nfft_set_tiling(nfft_plan* p, const int64_t* block_size, int row_
       set_error("block size must be positive");
       return NFFT_ERR_INVALID_ARG;
     }
-  if (row_parity_warps < 1 || row_parity_warps > 3) {
-    set_error("the spreading layout must be 1, 2 or 3");
+  if (row_parity_warps < 1 || row_parity_warps > 2) {
+    set_error("row_parity_warps must be 1 or 2");
     return NFFT_ERR_INVALID_ARG;
   }
   if (!p->has_nodes) {

@@ -131,7 +131,7 @@ struct nfft_plan {
   int4* tasks = nullptr;
   int spread_pitch = 0;            // shared-memory row pitch of the padded spreading tile
   int spread_layout = 1;           // D = 3 spreading kernel: 1 = 8 warps owning slices, 2 = 16 warps owning
-                                   // (slice group, row parity), 3 = register columns (FP32, spread_cols.cuh)
+                                   // (slice group, row parity)
   int gather_pitch = 0;            // shared-memory row pitch of the staged gather tile
   bool gather_tiled = false;       // gather from shared-memory tiles (else straight from L1/L2)
   int* dflag = nullptr;            // device status word
@@ -167,8 +167,6 @@ int launch_build_tasks(nfft_plan* p, int chunk);
 int apply_block_size(nfft_plan* p, const int64_t* bs, const void* k, int ny);
 // spread.cu: bank-conflict-free row pitch of a padded spreading tile
 int spread_pitch_for(int D, int m, int P0, int elem_bytes, int ny);
-// spread.cu: whether spreading layout 3 (register columns) runs this plan's tiles
-bool spread_cols_supported(const nfft_plan* p);
 // sort.cu
 int radix_sort_pairs(uint32_t* keys, int32_t* vals, uint32_t* keys_tmp, int32_t* vals_tmp, int64_t n,
                      int key_bits, void* scratch, size_t scratch_bytes, cudaStream_t s,

@@ -15,9 +15,6 @@
 //     ~17x the throughput of shared-memory float atomics on GB300), and can
 //     carry a Kahan compensation term (compensated = 1).  Nodes are staged in
 //     shared memory in batches (window values, x*y weight products, value);
-//   * D = 3, FP32, spreading layout 3 (spread_cols_kernel, spread_cols.cuh):
-//     the padded tile in registers, one z column per lane, no shared-memory
-//     accumulator traffic;
 //   * D = 1 (spread_pad1_kernel): 32/G nodes per warp, shared-memory atomics;
 //     compensated (spread_line_kahan_kernel): one warp per task, lane l owns
 //     the padded positions x = l mod 32, Kahan read-modify-writes;
@@ -25,9 +22,6 @@
 //     (red.global.add.v2), wrapping periodically; all-zero points are skipped.
 // The lock of the reference becomes the L2 atomics of the flush.
 #include "spread_body.cuh"
-#include "spread_cols.cuh"
-
-#include <type_traits>
 
 namespace nfft {
 namespace {
@@ -56,33 +50,6 @@ int sort_values(const nfft_plan* p, const typename Cplx<T>::type* fhat, typename
   if (nb > cap) nb = cap;
   if (nb < 1) nb = 1;
   sort_values_kernel<T><<<dim3(unsigned(nb), unsigned(ncols)), 256, 0, p->stream>>>(p->node4, fhat, out, p->M, fcol);
-  NFFT_LAUNCH_CHECK();
-  return NFFT_OK;
-}
-
-// Spreading layout 3 (D = 3, FP32): the padded tile in registers, one z
-// column per lane (spread_cols.cuh).  BZ = blockSize[3] in {8, 16}.
-template <int L>
-int spread_cols_launch(nfft_plan* p, const Geom<float>& G, const Nodes<float>& Nd, const float2* fp, float* gp,
-                       int ncols, int64_t fcol, int64_t gcol_t, void* sorted) {
-  if (!spread_cols_supported(p)) {
-    set_error("spreading layout 3 does not support this plan's tiles");
-    return NFFT_ERR_UNSUPPORTED;
-  }
-  float2* fs = static_cast<float2*>(ncols > 1 ? sorted : p->fsorted);
-  int rc = sort_values<float>(p, fp, fs, ncols, fcol);
-  if (rc) return rc;
-  const int nxb = col_xblocks(int(p->bs[0]), L), nyb = col_yblocks(int(p->bs[1]), L);
-  const int threads = 32 * nxb * nyb;
-  const int pair = (reinterpret_cast<uintptr_t>(gp) & 15) == 0 && (p->Nt[0] % 2) == 0 && (gcol_t % 4) == 0;
-  const dim3 grid(unsigned(p->n_tasks), unsigned(ncols));
-  if (p->bs[2] == 8) {
-    auto kern = p->wtab ? spread_cols_kernel<L, 8, true> : spread_cols_kernel<L, 8, false>;
-    kern<<<grid, threads, 0, p->stream>>>(G, Nd, p->tasks, fs, gp, nxb, pair, p->M, gcol_t);
-  } else {
-    auto kern = p->wtab ? spread_cols_kernel<L, 16, true> : spread_cols_kernel<L, 16, false>;
-    kern<<<grid, threads, 0, p->stream>>>(G, Nd, p->tasks, fs, gp, nxb, pair, p->M, gcol_t);
-  }
   NFFT_LAUNCH_CHECK();
   return NFFT_OK;
 }
@@ -131,9 +98,6 @@ int spread_launch(nfft_plan* p, const void* fhat, void* g, int ncols, int64_t fc
                                                                                           fcol, gcol_t);
   } else {
     const bool comp = p->prm.compensated != 0;
-    if constexpr (D == 3 && std::is_same<T, float>::value) {
-      if (p->spread_layout == 3) return spread_cols_launch<L>(p, G, Nd, fp, gp, ncols, fcol, gcol_t, sorted);
-    }
     const size_t smem = owned_smem<D, L, T>(p, comp);
     if (smem > 227 * 1024) {
       set_error("padded spreading tile (%zu bytes) does not fit in shared memory; use a smaller blockSize", smem);
@@ -215,13 +179,6 @@ int spread_pitch_for(int D, int m, int P0, int elem_bytes, int ny) {
     if (ok) return pitch;
   }
   return P0;
-}
-
-bool spread_cols_supported(const nfft_plan* p) {
-  if (p->D != 3 || p->precision != 32 || p->prm.compensated) return false;
-  if (p->bs[2] != 8 && p->bs[2] != 16) return false;
-  const int L = 2 * p->m;
-  return 32 * col_xblocks(int(p->bs[0]), L) * col_yblocks(int(p->bs[1]), L) <= kColMaxThreads;
 }
 
 int launch_spread(nfft_plan* p, const void* fhat, int, void* g, int) {

@@ -316,3 +316,4 @@ def test_paper_accuracy_d2_tensor_gpu_fp64():
         ra = np.mean(ea[m]) / oracle.PAPER_D2_TENSOR["adjoint"][m]
         assert 1 / 1.5 < rf < 1.5, (m, rf)
         assert 1 / 1.25 < ra < 1.25, (m, ra)
+
