@@ -3,6 +3,7 @@
 // include/nfft_gb300.h is public.
 #pragma once
 
+#include <cuda.h>
 #include <cuda_runtime.h>
 #include <cufft.h>
 #include <stdint.h>
@@ -132,6 +133,11 @@ struct nfft_plan {
   int spread_pitch = 0;            // shared-memory row pitch of the padded spreading tile
   int spread_layout = 1;           // D = 3 spreading kernel: 1 = 8 warps owning slices, 2 = 16 warps owning
                                    // (slice group, row parity)
+  bool spread_tile3 = true;        // 3-D FP32 m = 4: shape-specialised spreading kernel (spread_tile3.cuh)
+  bool spread_tma = true;          // its bulk tensor reduction flush for tiles that do not wrap
+  CUtensorMap tmap{};              // tensor map of the grid tmap_grid for that flush (shape tmap_key)
+  void* tmap_grid = nullptr;
+  int64_t tmap_key = 0;
   int gather_pitch = 0;            // shared-memory row pitch of the staged gather tile
   bool gather_tiled = false;       // gather from shared-memory tiles (else straight from L1/L2)
   int* dflag = nullptr;            // device status word

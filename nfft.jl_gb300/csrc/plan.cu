@@ -476,6 +476,9 @@ int nfft_plan_create(nfft_plan** out, int precision, int D, const int64_t* N, in
   p->gather_pitch = spread_pitch_for(D == 2 ? 3 : D, p->m, int(p->bs[0]) + 2 * p->m - 1,
                                      int(2 * (precision == 32 ? 4 : 8)), 1);
   if (const char* e = getenv("NFFT_GB300_GATHER_TILED")) p->gather_tiled = e[0] == '1';
+  // the shape-specialised 3-D spreader and its bulk-reduction flush (on by default)
+  if (const char* e = getenv("NFFT_GB300_SPREAD_TILE3")) p->spread_tile3 = e[0] != '0';
+  if (const char* e = getenv("NFFT_GB300_SPREAD_TMA")) p->spread_tma = e[0] != '0';
   p->ntiles_total = 1;
   for (int d = 0; d < 3; ++d) {
     p->ntiles[d] = (p->Nt[d] + p->bs[d] - 1) / p->bs[d];

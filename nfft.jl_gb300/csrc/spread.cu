@@ -22,6 +22,9 @@
 //     (red.global.add.v2), wrapping periodically; all-zero points are skipped.
 // The lock of the reference becomes the L2 atomics of the flush.
 #include "spread_body.cuh"
+#include "spread_tile3.cuh"
+
+#include <mutex>
 
 namespace nfft {
 namespace {
@@ -52,6 +55,79 @@ int sort_values(const nfft_plan* p, const typename Cplx<T>::type* fhat, typename
   sort_values_kernel<T><<<dim3(unsigned(nb), unsigned(ncols)), 256, 0, p->stream>>>(p->node4, fhat, out, p->M, fcol);
   NFFT_LAUNCH_CHECK();
   return NFFT_OK;
+}
+
+using EncodeTiledFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                   const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+// cuTensorMapEncodeTiled through the runtime's driver entry point (the
+// library does not link the driver library itself); null if unavailable.
+EncodeTiledFn encode_tiled() {
+  static EncodeTiledFn fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q{};
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<EncodeTiledFn>(f);
+  });
+  return fn;
+}
+
+// Tensor map of the FP32 grid g (2 Ntilde[0] floats x Ntilde[1] x Ntilde[2])
+// with the padded-tile box of Tile3<BX, BY, BZ>, cached on the plan per grid
+// and shape.  False when it cannot be made (no driver entry point, grid not
+// 16-byte aligned, box larger than the grid): the kernel then flushes per point.
+template <int BX, int BY, int BZ> bool tile3_map(nfft_plan* p, void* g) {
+  using TC = Tile3<BX, BY, BZ>;
+  const int64_t key = (int64_t(BX) << 20) | (int64_t(BY) << 10) | BZ;
+  if (p->tmap_grid == g && p->tmap_key == key) return true;
+  p->tmap_grid = nullptr;
+  EncodeTiledFn fn = encode_tiled();
+  if (!fn || (reinterpret_cast<uintptr_t>(g) & 15) != 0) return false;
+  if (p->Nt[0] < TC::PITCH || p->Nt[1] < TC::P1 || p->Nt[2] < TC::P2) return false;
+  const cuuint64_t dims[3] = {cuuint64_t(2 * p->Nt[0]), cuuint64_t(p->Nt[1]), cuuint64_t(p->Nt[2])};
+  const cuuint64_t strides[2] = {cuuint64_t(8 * p->Nt[0]), cuuint64_t(8 * p->Nt[0] * p->Nt[1])};
+  const cuuint32_t box[3] = {cuuint32_t(2 * TC::PITCH), cuuint32_t(TC::P1), cuuint32_t(TC::P2)};
+  const cuuint32_t es[3] = {1, 1, 1};
+  if (fn(&p->tmap, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, g, dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
+         CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) !=
+      CUDA_SUCCESS)
+    return false;
+  p->tmap_grid = g;
+  p->tmap_key = key;
+  return true;
+}
+
+template <int BX, int BY, int BZ>
+int tile3_launch(nfft_plan* p, const Geom<float>& G, const Nodes<float>& Nd, const float2* fs, float* gp, int ncols,
+                 int64_t fcol, int64_t gcol_t) {
+  using TC = Tile3<BX, BY, BZ>;
+  const int use_tma = (ncols == 1 && p->spread_tma && tile3_map<BX, BY, BZ>(p, gp)) ? 1 : 0;
+  auto kern = p->wtab ? spread_tile3_kernel<BX, BY, BZ, true> : spread_tile3_kernel<BX, BY, BZ, false>;
+  NFFT_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(TC::SMEM)));
+  CUtensorMap none{};
+  kern<<<dim3(unsigned(p->n_tasks), unsigned(ncols)), TC::THREADS, TC::SMEM, p->stream>>>(
+      use_tma ? p->tmap : none, use_tma, G, Nd, p->tasks, fs, gp, ncols > 1 ? fcol : 0, gcol_t);
+  NFFT_LAUNCH_CHECK();
+  return NFFT_OK;
+}
+
+// The shape-specialised 3-D kernel when the plan's tiles have one of its
+// shapes (FP32, m = 4, uncompensated, 8-warp layout); -1 = not applicable.
+int spread_tile3(nfft_plan* p, const Geom<float>& G, const Nodes<float>& Nd, const float2* fs, float* gp, int ncols,
+                 int64_t fcol, int64_t gcol_t) {
+  if (!p->spread_tile3 || p->D != 3 || p->m != 4 || p->prm.compensated || p->spread_layout != 1) return -1;
+  const int64_t bx = p->bs[0], by = p->bs[1], bz = p->bs[2];
+  if (bz != 8) return -1;
+  if (bx == 16 && by == 8) return tile3_launch<16, 8, 8>(p, G, Nd, fs, gp, ncols, fcol, gcol_t);
+  if (bx == 16 && by == 16) return tile3_launch<16, 16, 8>(p, G, Nd, fs, gp, ncols, fcol, gcol_t);
+  if (bx == 32 && by == 8) return tile3_launch<32, 8, 8>(p, G, Nd, fs, gp, ncols, fcol, gcol_t);
+  if (bx == 8 && by == 8) return tile3_launch<8, 8, 8>(p, G, Nd, fs, gp, ncols, fcol, gcol_t);
+  return -1;
 }
 
 // ncols columns in one launch (blockIdx.y): values fhat + c fcol, grids
@@ -116,6 +192,10 @@ int spread_launch(nfft_plan* p, const void* fhat, void* g, int ncols, int64_t fc
     C* fs = static_cast<C*>(ncols > 1 ? sorted : p->fsorted);
     int rc = sort_values<T>(p, fp, fs, ncols, fcol);
     if (rc) return rc;
+    if constexpr (D == 3 && L == 8 && sizeof(T) == 4) {
+      rc = spread_tile3(p, G, Nd, fs, gp, ncols, p->M, gcol_t);
+      if (rc != -1) return rc;
+    }
     kern<<<dim3(unsigned(p->n_tasks), unsigned(ncols)), threads, smem, p->stream>>>(G, Nd, p->tasks, fs, gp,
                                                                                    p->spread_pitch, p->M, gcol_t);
   }

@@ -1,0 +1,193 @@
+// Shape-specialised slice-owned spreading for 3-D FP32 plans with m = 4
+// (2m = 8 taps per dimension) and tile shapes fixed at compile time.
+//
+// The algorithm is the slice-owned kernel of spread_body.cuh (warp w owns the
+// z slices w mod 8 of the tile padded by 2m - 1 points, atomic-free
+// read-modify-writes in shared memory), specialised so that the tap loop is
+// almost only its memory operations and FFMAs:
+//   * the padded tile's row pitch is a constant, so a lane's two taps of a
+//     node (rows iy and iy + 4) are one base address plus immediate offsets,
+//     and every lane is active in both steps (8 x 4 lanes, 8 rows);
+//   * with 8 owner warps and 8 taps along z every warp owns exactly one slice
+//     of every node: no ownership or activity tests;
+//   * staging computes the 64 x-y weight products of a node one window row
+//     per thread;
+//   * the padded tile starts at the even grid x o0 - m (one leading column
+//     that stays zero), so it is laid out as a TMA box: a tile that does not
+//     wrap around the grid is added to it by one bulk tensor reduction
+//     (cp.reduce.async.bulk.tensor ... .add) issued by one thread, instead of
+//     ~2700 vector atomics spread over the CTA; tiles that wrap (and grids
+//     without a tensor map) use the per-point flush of spread_body.cuh.
+#pragma once
+
+#include <cuda.h>  // CUtensorMap (encoded on the host through the runtime's driver entry point)
+
+#include "spread_body.cuh"
+
+namespace nfft {
+namespace {
+
+template <int BX, int BY, int BZ> struct Tile3 {
+  static constexpr int L = 8;
+  static constexpr int P0 = BX + L;                      // columns, from grid x o0 - m
+  static constexpr int PITCH = P0 + ((8 - P0 % 16) + 16) % 16;  // >= P0, = 8 mod 16: conflict-free row pairs
+  static constexpr int P1 = BY + L - 1;
+  static constexpr int P2 = BZ + L - 1;
+  static constexpr int PLANE = PITCH * P1;
+  static constexpr int NACC = PLANE * P2;                // float2 accumulators
+  static constexpr int THREADS = 256;
+  static constexpr int NB = 32;                          // nodes per staged batch
+  static constexpr size_t ACC_BYTES = (size_t(NACC) * 8 + 127) & ~size_t(127);
+  static constexpr size_t SMEM = ACC_BYTES + size_t(NB) * (16 + 8 + 8 * L + 4 * 3 * L + 4 * L * L);
+  static_assert(PITCH <= 128 && P1 <= 256 && P2 <= 256, "TMA box extents");
+};
+
+// The grid region of a tile's padded box lies inside the grid (no wrap):
+// the box is added with one bulk tensor reduction.
+template <int BX, int BY, int BZ>
+__device__ __forceinline__ bool tile3_interior(const Geom<float>& G, int o0, int o1, int o2) {
+  using TC = Tile3<BX, BY, BZ>;
+  const int x = o0 - 4, y = o1 - 3, z = o2 - 3;
+  return x >= 0 && y >= 0 && z >= 0 && x + TC::PITCH <= G.Nt[0] && y + TC::P1 <= G.Nt[1] && z + TC::P2 <= G.Nt[2];
+}
+
+template <int BX, int BY, int BZ, bool TABLE>
+__global__ void __launch_bounds__(256) spread_tile3_kernel(const __grid_constant__ CUtensorMap tmap, int use_tma,
+                                                            Geom<float> G, Nodes<float> Nd,
+                                                            const int4* __restrict__ tasks,
+                                                            const float2* __restrict__ fsorted,
+                                                            float* __restrict__ g, int64_t fcol, int64_t gcol) {
+  using TC = Tile3<BX, BY, BZ>;
+  constexpr int L = TC::L, NB = TC::NB, DL = 3 * L, DEG = L + 1;
+  constexpr int PITCH = TC::PITCH, PLANE = TC::PLANE;
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  fsorted += blockIdx.y * fcol;  // column of a multi-column launch
+  g += blockIdx.y * gcol;
+  float2* acc = reinterpret_cast<float2*>(smem_raw);
+  int4* s_meta = reinterpret_cast<int4*>(smem_raw + TC::ACC_BYTES);  // {row/column offset, z offset}
+  float2* s_c = reinterpret_cast<float2*>(s_meta + NB);                // [NB]
+  float2* s_cz = s_c + NB;                                             // [NB][L]: value x z window value
+  float* s_w = reinterpret_cast<float*>(s_cz + NB * L);                // [NB][3L]
+  float* s_xy = s_w + NB * DL;                                         // [NB][L * L]
+  const int4 task = tasks[blockIdx.x];
+  const int tile = task.x;
+  const int tc0 = tile % G.ntiles[0];
+  const int tc1 = (tile / G.ntiles[0]) % G.ntiles[1];
+  const int tc2 = tile / (G.ntiles[0] * G.ntiles[1]);
+  const int o0 = tc0 * BX, o1 = tc1 * BY, o2 = tc2 * BZ;
+  {
+    float4* a4 = reinterpret_cast<float4*>(acc);
+    for (int q = threadIdx.x; q < TC::NACC / 2; q += TC::THREADS) a4[q] = make_float4(0.f, 0.f, 0.f, 0.f);
+  }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int lofs = (lane >> 3) * PITCH + (lane & 7);  // this lane's tap (x = lane mod 8, row = lane / 8)
+
+  // register prefetch of one batch: node, value, window values (or fractional offsets)
+  constexpr int WPT = NB * DL / TC::THREADS;  // 3
+  int4 r_nd = make_int4(0, 0, 0, 0);
+  float2 r_c = make_float2(0.f, 0.f);
+  float r_w[WPT];
+  auto prefetch = [&](int b) {
+    const int n = min(NB, task.z - b);
+    if (threadIdx.x < n) {
+      r_nd = __ldg(Nd.node4 + b + threadIdx.x);
+      r_c = __ldg(fsorted + b + threadIdx.x);
+    }
+#pragma unroll
+    for (int u = 0; u < WPT; ++u) {
+      const int q = threadIdx.x + u * TC::THREADS;
+      if (q < n * DL) {
+        if constexpr (TABLE) r_w[u] = __ldg(Nd.wtab + int64_t(b) * DL + q);
+        else r_w[u] = __ldg(Nd.frac4 + 4 * int64_t(b + q / DL) + (q % DL) / L);
+      }
+    }
+  };
+  if (task.y < task.z) prefetch(task.y);
+  __syncthreads();
+
+  for (int b = task.y; b < task.z; b += NB) {
+    const int n = min(NB, task.z - b);
+    // stage 1: registers -> shared (window values evaluated here for POLYNOMIAL)
+    if (threadIdx.x < n) {
+      s_meta[threadIdx.x] = make_int4((r_nd.y - o1) * PITCH + (r_nd.x - o0 + 1), r_nd.z - o2, 0, 0);
+      s_c[threadIdx.x] = r_c;
+    }
+#pragma unroll
+    for (int u = 0; u < WPT; ++u) {
+      const int q = threadIdx.x + u * TC::THREADS;
+      if (q < n * DL) {
+        float w = r_w[u];
+        if constexpr (!TABLE) {
+          const int l = (q % DL) % L;
+          const float t = w - 0.5f;
+          const float* c = G.coeffs + l * DEG;
+          w = __ldg(c + DEG - 1);
+#pragma unroll
+          for (int i = DEG - 2; i >= 0; --i) w = fmaf(w, t, __ldg(c + i));
+        }
+        s_w[q] = w;
+      }
+    }
+    __syncthreads();
+    // stage 2: thread (node s, row iy): the row of x-y products and c * wz[iy]
+    {
+      const int s = threadIdx.x >> 3, iy = threadIdx.x & 7;
+      if (s < n) {
+        const float* ws = s_w + s * DL;
+        const float wyv = ws[L + iy];
+        const float4 x0 = *reinterpret_cast<const float4*>(ws);
+        const float4 x1 = *reinterpret_cast<const float4*>(ws + 4);
+        float4* out = reinterpret_cast<float4*>(s_xy + s * L * L + iy * L);
+        out[0] = make_float4(x0.x * wyv, x0.y * wyv, x0.z * wyv, x0.w * wyv);
+        out[1] = make_float4(x1.x * wyv, x1.y * wyv, x1.z * wyv, x1.w * wyv);
+        const float wz = ws[2 * L + iy];
+        const float2 c = s_c[s];
+        s_cz[s * L + iy] = make_float2(c.x * wz, c.y * wz);
+      }
+    }
+    __syncthreads();
+    if (b + NB < task.z) prefetch(b + NB);
+    // taps: warp w updates its slice of every node, rows iy and iy + 4 of the
+    // lane's column; the next node's record is loaded during this node's taps
+    int4 mt = s_meta[0];
+    for (int s = 0; s < n; ++s) {
+      const int4 mn = s_meta[s + 1 < n ? s + 1 : s];
+      const int is = (warp - mt.y) & 7;
+      float2* p = acc + (mt.y + is) * PLANE + mt.x + lofs;
+      const float* xy = s_xy + s * L * L + lane;
+      const float2 cz = s_cz[s * L + is];
+      float2 a0 = p[0], a1 = p[4 * PITCH];
+      const float w0 = xy[0], w1 = xy[32];
+      a0.x = fmaf(cz.x, w0, a0.x);
+      a0.y = fmaf(cz.y, w0, a0.y);
+      a1.x = fmaf(cz.x, w1, a1.x);
+      a1.y = fmaf(cz.y, w1, a1.y);
+      p[0] = a0;
+      p[4 * PITCH] = a1;
+      mt = mn;
+    }
+    __syncthreads();
+  }
+  // the tile's shared-memory writes, made visible to the bulk (async) copy
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  __syncthreads();
+
+  if (use_tma && tile3_interior<BX, BY, BZ>(G, o0, o1, o2)) {
+    if (threadIdx.x == 0) {
+      const int x = 2 * (o0 - 4), y = o1 - 3, z = o2 - 3;  // x in floats: a multiple of 4 (16 bytes)
+      const unsigned src = static_cast<unsigned>(__cvta_generic_to_shared(acc));
+      asm volatile(
+          "cp.reduce.async.bulk.tensor.3d.global.shared::cta.add.tile.bulk_group [%0, {%1, %2, %3}], [%4];"
+          ::"l"(reinterpret_cast<uint64_t>(&tmap)), "r"(x), "r"(y), "r"(z), "r"(src)
+          : "memory");
+      asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+      asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");  // the tile has been read before exit
+    }
+    return;
+  }
+  // wrapping tiles: per-point flush from padded column 1 (grid x o0 - m + 1)
+  flush_tile<3, float, false, 8>(G, acc + 1, g, o0, o1, o2, TC::P0 - 1, TC::P1, TC::P2, PITCH);
+}
+
+}  // namespace
+}  // namespace nfft

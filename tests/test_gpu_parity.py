@@ -317,3 +317,28 @@ def test_paper_accuracy_d2_tensor_gpu_fp64():
         assert 1 / 1.5 < rf < 1.5, (m, rf)
         assert 1 / 1.25 < ra < 1.25, (m, ra)
 
+
+
+@pytest.mark.parametrize("bs", [(16, 8, 8), (16, 16, 8), (32, 8, 8), (8, 8, 8)])
+@pytest.mark.parametrize("pre", [oracle.TENSOR, oracle.POLYNOMIAL])
+@pytest.mark.parametrize("path", ["tma", "points", "generic"])
+def test_specialised_3d_spreader(monkeypatch, bs, pre, path):
+    """The shape-specialised 3-D FP32 m = 4 spreader, with the bulk tensor
+    reduction flush for tiles inside the grid ("tma"), with the per-point
+    flush only ("points"), and the generic kernel ("generic"), all give the
+    oracle's adjoint; the grid has interior tiles and tiles that wrap in every
+    dimension, boundary nodes included."""
+    monkeypatch.setenv("NFFT_GB300_SPREAD_TILE3", "0" if path == "generic" else "1")
+    monkeypatch.setenv("NFFT_GB300_SPREAD_TMA", "1" if path == "tma" else "0")
+    N = (48, 40, 36)
+    k, f, fhat = rand_problem(3, N, 30000, seed=300, dtype=np.float32)
+    k[:, :5] = np.array([[-0.5, 0.4999, 0.0, -0.001, 0.25]] * 3, dtype=np.float32)
+    p = nf.plan_nfft(k, N, m=4, sigma=2.0, precompute=pre, blockSize=bs)
+    op = oracle.OraclePlan(k.astype(np.float64), N, m=4, sigma=2.0, precompute=pre)
+    x = (nf.adjoint(p) * torch.as_tensor(fhat).to(p.cdtype)).cpu().numpy()
+    assert oracle.rel_l2(colmajor_flat(x), colmajor_flat(op.adjoint(fhat))) < TOL32
+    # convolve_transpose! into a caller's grid (tensor map of that grid)
+    g = torch.zeros(p.Ñ[::-1], dtype=p.cdtype, device="cuda").permute(2, 1, 0)
+    p.convolve_transpose_(torch.as_tensor(fhat).to(p.cdtype).cuda(), g)
+    ref = op.convolve_transpose(fhat.astype(np.complex128))
+    assert oracle.rel_l2(colmajor_flat(g.cpu().numpy()), colmajor_flat(ref)) < TOL32
