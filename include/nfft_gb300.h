@@ -376,7 +376,10 @@ int nfft_nnplan_forward(nfft_nnplan* plan, const void* c, void* fhat);
 /* fhat (M complex) -> c (Ny complex) */
 int nfft_nnplan_adjoint(nfft_nnplan* plan, const void* fhat, void* c);
 
-/* Wait for the plan's stream. */
+/* Wait for the plan's stream.  Returns NFFT_ERR_TIMEOUT (once) if a kernel
+ * of the plan gave up waiting for a bulk tensor copy into shared memory
+ * (bounded waits: the kernel skips the work it was waiting for instead of
+ * spinning forever). */
 int nfft_sync(nfft_plan* plan);
 
 /* Number of kernels this library has launched in the calling process. */

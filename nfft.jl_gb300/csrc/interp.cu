@@ -10,6 +10,7 @@
 // its coefficients held in registers (POLYNOMIAL).  Grid offsets within a
 // plane are 32-bit; the plane offset is 64-bit.
 #include "interp_body.cuh"
+#include "tile3.cuh"
 
 namespace nfft {
 namespace {
@@ -247,6 +248,144 @@ __global__ void __launch_bounds__(kInterpThreads) interp_tile_kernel(Geom<T> G, 
   }
 }
 
+// ---------------------------------------------------------------------------
+// Shape-specialised 3-D FP32 gather (m = 4, the tiles of tile3.cuh).  One CTA
+// per spreading task; a tile whose padded box lies inside the grid is brought
+// into shared memory by one bulk tensor copy (TMA, completion on an
+// mbarrier), and each warp then interpolates one node at a time from shared
+// memory: lane (x = lane mod 8, row = lane / 8) reads its 8 z values of rows
+// iy and iy + 4 at constant offsets (16 loads, 2 wavefronts each), sums over
+// z, weights by phi_x phi_y and the warp adds the 32 partial sums.  Tiles
+// whose box wraps around the grid gather their nodes straight from L1/L2 as
+// interp_kernel does.  The wait for the copy is bounded: on timeout the CTA
+// raises status word 1 (reported by nfft_sync) and skips its nodes.
+
+__device__ __forceinline__ void mbar_init(unsigned addr, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(addr), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(unsigned addr, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(addr), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(unsigned addr, unsigned parity) {
+  unsigned ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+      : "=r"(ok)
+      : "r"(addr), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+template <int BX, int BY, int BZ, bool TABLE>
+__global__ void __launch_bounds__(kInterpThreads) interp_tile3_kernel(const __grid_constant__ CUtensorMap tmap,
+                                                                       Geom<float> G, Nodes<float> Nd,
+                                                                       const int4* __restrict__ tasks,
+                                                                       const float2* __restrict__ g,
+                                                                       float2* __restrict__ fhat, int* status) {
+  using TC = Tile3<BX, BY, BZ>;
+  using LN = Lanes<3, 8>;
+  constexpr int PITCH = TC::PITCH, PLANE = TC::PLANE;
+  constexpr unsigned BOX_BYTES = unsigned(2 * PITCH) * 4u * TC::P1 * TC::P2;
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  float2* tile = reinterpret_cast<float2*>(smem_raw);
+  uint64_t* mbar = reinterpret_cast<uint64_t*>(smem_raw + TC::ACC_BYTES);
+  const int4 task = tasks[blockIdx.x];
+  const int t = task.x;
+  const int tc0 = t % G.ntiles[0];
+  const int tc1 = (t / G.ntiles[0]) % G.ntiles[1];
+  const int tc2 = t / (G.ntiles[0] * G.ntiles[1]);
+  const int o0 = tc0 * BX, o1 = tc1 * BY, o2 = tc2 * BZ;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  constexpr int NWARPS = kInterpThreads / 32;
+  PolyRegs<3, 8, float> P;
+  if constexpr (!TABLE) P.load(G.coeffs, lane);
+  const unsigned tile_s = static_cast<unsigned>(__cvta_generic_to_shared(tile));
+  const unsigned mbar_s = static_cast<unsigned>(__cvta_generic_to_shared(mbar));
+  // the bulk copy's shared-memory destination must be 128-byte aligned
+  if (!tile3_interior<BX, BY, BZ>(G, o0, o1, o2) || (tile_s & 127u) != 0) {
+    for (int64_t i = task.y + warp; i < task.z; i += NWARPS) interp_node<3, 8, float, TABLE>(G, Nd, P, i, lane, g, fhat);
+    return;
+  }
+  if (threadIdx.x == 0) {
+    mbar_init(mbar_s, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    mbar_expect_tx(mbar_s, BOX_BYTES);
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
+        "[%5];" ::"r"(tile_s),
+        "l"(reinterpret_cast<uint64_t>(&tmap)), "r"(2 * (o0 - 4)), "r"(o1 - 3), "r"(o2 - 3), "r"(mbar_s)
+        : "memory");
+  }
+  bool done = false;
+  for (int it = 0; it < (1 << 22) && !done; ++it) done = mbar_try_wait(mbar_s, 0);
+  if (!done) {
+    if (threadIdx.x == 0) atomicOr(status, 1);
+    return;
+  }
+  const int ix = lane & 7, ry = lane >> 3;
+  for (int64_t i = task.y + warp; i < task.z; i += NWARPS) {
+    const int4 nd = __ldg(Nd.node4 + i);
+    float W[LN::NW];
+    node_weights<3, 8, float, TABLE>(Nd, P, i, lane, W);
+    const float wx = wsel<3, 8>(W, ix);
+    const float wy0 = wsel<3, 8>(W, 8 + ry), wy1 = wsel<3, 8>(W, 12 + ry);
+    const float2* base = tile + (nd.z - o2) * PLANE + (nd.y - o1 + ry) * PITCH + (nd.x - o0 + 1) + ix;
+    float2 v0[8], v1[8];
+#pragma unroll
+    for (int iz = 0; iz < 8; ++iz) {
+      v0[iz] = base[iz * PLANE];
+      v1[iz] = base[iz * PLANE + 4 * PITCH];
+    }
+    float s0r = 0.f, s0i = 0.f, s1r = 0.f, s1i = 0.f;
+#pragma unroll
+    for (int iz = 0; iz < 8; ++iz) {
+      const float wz = wsel<3, 8>(W, 16 + iz);
+      s0r = fmaf(wz, v0[iz].x, s0r);
+      s0i = fmaf(wz, v0[iz].y, s0i);
+      s1r = fmaf(wz, v1[iz].x, s1r);
+      s1i = fmaf(wz, v1[iz].y, s1i);
+    }
+    float ar = wx * fmaf(wy0, s0r, wy1 * s1r);
+    float ai = wx * fmaf(wy0, s0i, wy1 * s1i);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      ar += __shfl_xor_sync(0xFFFFFFFFu, ar, o);
+      ai += __shfl_xor_sync(0xFFFFFFFFu, ai, o);
+    }
+    if (lane == 0) fhat[nd.w] = make_float2(ar, ai);
+  }
+}
+
+template <int BX, int BY, int BZ>
+int interp_tile3_launch(const nfft_plan* p, const Geom<float>& G, const Nodes<float>& Nd, const float2* g,
+                        float2* fhat) {
+  using TC = Tile3<BX, BY, BZ>;
+  const size_t smem = TC::ACC_BYTES + 16;
+  auto kern = p->wtab ? interp_tile3_kernel<BX, BY, BZ, true> : interp_tile3_kernel<BX, BY, BZ, false>;
+  NFFT_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
+  kern<<<unsigned(p->n_tasks), kInterpThreads, smem, p->stream>>>(p->tmap, G, Nd, p->tasks, g, fhat, p->dflag + 1);
+  NFFT_LAUNCH_CHECK();
+  return NFFT_OK;
+}
+
+// The TMA-tiled 3-D gather when the plan has one of the fixed tile shapes and
+// the grid's tensor map can be made; -1 = not applicable.
+int interp_tile3(const nfft_plan* cp, const Geom<float>& G, const Nodes<float>& Nd, const float2* g, float2* fhat) {
+  nfft_plan* p = const_cast<nfft_plan*>(cp);  // the tensor-map cache only
+  if (!p->gather_tma || !p->tasks || p->n_tasks == 0 || !tile3_shape(p)) return -1;
+  void* gv = const_cast<float2*>(g);
+  const int64_t bx = p->bs[0], by = p->bs[1];
+  if (bx == 16 && by == 8) return tile3_map<16, 8, 8>(p, gv) ? interp_tile3_launch<16, 8, 8>(p, G, Nd, g, fhat) : -1;
+  if (bx == 16 && by == 16)
+    return tile3_map<16, 16, 8>(p, gv) ? interp_tile3_launch<16, 16, 8>(p, G, Nd, g, fhat) : -1;
+  if (bx == 32 && by == 8) return tile3_map<32, 8, 8>(p, gv) ? interp_tile3_launch<32, 8, 8>(p, G, Nd, g, fhat) : -1;
+  if (bx == 8 && by == 8) return tile3_map<8, 8, 8>(p, gv) ? interp_tile3_launch<8, 8, 8>(p, G, Nd, g, fhat) : -1;
+  return -1;
+}
+
 // ncols columns in one launch (blockIdx.y): grids g + c gcol, values fhat + c fcol.
 template <int D, int L, typename T>
 int interp_launch(const nfft_plan* p, const void* g, void* fhat, int ncols, int64_t gcol, int64_t fcol) {
@@ -256,7 +395,11 @@ int interp_launch(const nfft_plan* p, const void* g, void* fhat, int ncols, int6
   using C = typename Cplx<T>::type;
   const int64_t per_block = (kInterpThreads / 32) * (D == 1 ? Lanes<D, L>::NPW : 1);
   int64_t blocks = (Nd.M + per_block - 1) / per_block;
-  const int64_t cap = (152 * 64 + ncols - 1) / ncols;
+  int dev = 0, sms = 1;
+  if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) !=
+                                                cudaSuccess || sms < 1)
+    sms = 1;
+  const int64_t cap = (int64_t(sms) * 64 + ncols - 1) / ncols;
   if (blocks > cap) blocks = cap;
   const C* gp = static_cast<const C*>(g);
   C* fp = static_cast<C*>(fhat);
@@ -268,6 +411,10 @@ int interp_launch(const nfft_plan* p, const void* g, void* fhat, int ncols, int6
       interp_kernel<D, L, T, false, true><<<grid, kInterpThreads, 0, p->stream>>>(G, Nd, gp, fp, gcol, fcol);
     NFFT_LAUNCH_CHECK();
     return NFFT_OK;
+  }
+  if constexpr (D == 3 && L == 8 && sizeof(T) == 4) {
+    const int rc = interp_tile3(p, G, Nd, gp, fp);
+    if (rc != -1) return rc;
   }
   if (p->tasks && p->gather_tiled) {
     const int P1 = D >= 2 ? int(p->bs[1]) + L - 1 : 1;

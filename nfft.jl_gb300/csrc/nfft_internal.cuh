@@ -135,12 +135,13 @@ struct nfft_plan {
                                    // (slice group, row parity)
   bool spread_tile3 = true;        // 3-D FP32 m = 4: shape-specialised spreading kernel (spread_tile3.cuh)
   bool spread_tma = true;          // its bulk tensor reduction flush for tiles that do not wrap
+  bool gather_tma = true;          // 3-D FP32 m = 4 gather from tiles loaded by bulk tensor copies
   CUtensorMap tmap{};              // tensor map of the grid tmap_grid for that flush (shape tmap_key)
   void* tmap_grid = nullptr;
   int64_t tmap_key = 0;
   int gather_pitch = 0;            // shared-memory row pitch of the staged gather tile
   bool gather_tiled = false;       // gather from shared-memory tiles (else straight from L1/L2)
-  int* dflag = nullptr;            // device status word
+  int* dflag = nullptr;            // device status words: [0] node check, [1] an async copy wait that timed out
   size_t scratch_bytes = 0;
 
   // TimingStats: every forward/adjoint records 4 events into a ring slot; the

@@ -479,6 +479,7 @@ int nfft_plan_create(nfft_plan** out, int precision, int D, const int64_t* N, in
   // the shape-specialised 3-D spreader and its bulk-reduction flush (on by default)
   if (const char* e = getenv("NFFT_GB300_SPREAD_TILE3")) p->spread_tile3 = e[0] != '0';
   if (const char* e = getenv("NFFT_GB300_SPREAD_TMA")) p->spread_tma = e[0] != '0';
+  if (const char* e = getenv("NFFT_GB300_GATHER_TMA")) p->gather_tma = e[0] != '0';
   p->ntiles_total = 1;
   for (int d = 0; d < 3; ++d) {
     p->ntiles[d] = (p->Nt[d] + p->bs[d] - 1) / p->bs[d];
@@ -502,7 +503,7 @@ int nfft_plan_create(nfft_plan** out, int precision, int D, const int64_t* N, in
   const int64_t ninv = p->N[0] + (D > 1 ? p->N[1] : 0) + (D > 2 ? p->N[2] : 0) + 1;
   const int deg = 2 * p->m + 1, L = 2 * p->m;
   if (cudaMalloc(&p->inv, rs * ninv) != cudaSuccess || cudaMalloc(&p->coeffs, rs * deg * L) != cudaSuccess ||
-      cudaMalloc(&p->dflag, sizeof(int)) != cudaSuccess) {
+      cudaMalloc(&p->dflag, 2 * sizeof(int)) != cudaSuccess || cudaMemset(p->dflag, 0, 2 * sizeof(int)) != cudaSuccess) {
     set_error("cudaMalloc of plan tables failed");
     return fail(NFFT_ERR_ALLOC);
   }
@@ -917,6 +918,13 @@ int nfft_get_deconv_factors(nfft_plan* p, void* out) {
 int nfft_sync(nfft_plan* p) {
   if (!p) return NFFT_ERR_INVALID_ARG;
   NFFT_CUDA_TRY(cudaStreamSynchronize(p->stream));
+  int st = 0;
+  NFFT_CUDA_TRY(cudaMemcpy(&st, p->dflag + 1, sizeof(int), cudaMemcpyDeviceToHost));
+  if (st) {
+    NFFT_CUDA_TRY(cudaMemset(p->dflag + 1, 0, sizeof(int)));
+    set_error("a bulk tensor copy into shared memory did not complete within its wait limit");
+    return NFFT_ERR_TIMEOUT;
+  }
   return NFFT_OK;
 }
 

@@ -24,8 +24,6 @@
 #include "spread_body.cuh"
 #include "spread_tile3.cuh"
 
-#include <mutex>
-
 namespace nfft {
 namespace {
 
@@ -55,51 +53,6 @@ int sort_values(const nfft_plan* p, const typename Cplx<T>::type* fhat, typename
   sort_values_kernel<T><<<dim3(unsigned(nb), unsigned(ncols)), 256, 0, p->stream>>>(p->node4, fhat, out, p->M, fcol);
   NFFT_LAUNCH_CHECK();
   return NFFT_OK;
-}
-
-using EncodeTiledFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
-                                   const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
-                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
-
-// cuTensorMapEncodeTiled through the runtime's driver entry point (the
-// library does not link the driver library itself); null if unavailable.
-EncodeTiledFn encode_tiled() {
-  static EncodeTiledFn fn = nullptr;
-  static std::once_flag once;
-  std::call_once(once, [] {
-    void* f = nullptr;
-    cudaDriverEntryPointQueryResult q{};
-    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) ==
-            cudaSuccess &&
-        q == cudaDriverEntryPointSuccess)
-      fn = reinterpret_cast<EncodeTiledFn>(f);
-  });
-  return fn;
-}
-
-// Tensor map of the FP32 grid g (2 Ntilde[0] floats x Ntilde[1] x Ntilde[2])
-// with the padded-tile box of Tile3<BX, BY, BZ>, cached on the plan per grid
-// and shape.  False when it cannot be made (no driver entry point, grid not
-// 16-byte aligned, box larger than the grid): the kernel then flushes per point.
-template <int BX, int BY, int BZ> bool tile3_map(nfft_plan* p, void* g) {
-  using TC = Tile3<BX, BY, BZ>;
-  const int64_t key = (int64_t(BX) << 20) | (int64_t(BY) << 10) | BZ;
-  if (p->tmap_grid == g && p->tmap_key == key) return true;
-  p->tmap_grid = nullptr;
-  EncodeTiledFn fn = encode_tiled();
-  if (!fn || (reinterpret_cast<uintptr_t>(g) & 15) != 0) return false;
-  if (p->Nt[0] < TC::PITCH || p->Nt[1] < TC::P1 || p->Nt[2] < TC::P2) return false;
-  const cuuint64_t dims[3] = {cuuint64_t(2 * p->Nt[0]), cuuint64_t(p->Nt[1]), cuuint64_t(p->Nt[2])};
-  const cuuint64_t strides[2] = {cuuint64_t(8 * p->Nt[0]), cuuint64_t(8 * p->Nt[0] * p->Nt[1])};
-  const cuuint32_t box[3] = {cuuint32_t(2 * TC::PITCH), cuuint32_t(TC::P1), cuuint32_t(TC::P2)};
-  const cuuint32_t es[3] = {1, 1, 1};
-  if (fn(&p->tmap, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, g, dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
-         CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) !=
-      CUDA_SUCCESS)
-    return false;
-  p->tmap_grid = g;
-  p->tmap_key = key;
-  return true;
 }
 
 template <int BX, int BY, int BZ>

@@ -20,36 +20,11 @@
 //     without a tensor map) use the per-point flush of spread_body.cuh.
 #pragma once
 
-#include <cuda.h>  // CUtensorMap (encoded on the host through the runtime's driver entry point)
-
 #include "spread_body.cuh"
+#include "tile3.cuh"
 
 namespace nfft {
 namespace {
-
-template <int BX, int BY, int BZ> struct Tile3 {
-  static constexpr int L = 8;
-  static constexpr int P0 = BX + L;                      // columns, from grid x o0 - m
-  static constexpr int PITCH = P0 + ((8 - P0 % 16) + 16) % 16;  // >= P0, = 8 mod 16: conflict-free row pairs
-  static constexpr int P1 = BY + L - 1;
-  static constexpr int P2 = BZ + L - 1;
-  static constexpr int PLANE = PITCH * P1;
-  static constexpr int NACC = PLANE * P2;                // float2 accumulators
-  static constexpr int THREADS = 256;
-  static constexpr int NB = 32;                          // nodes per staged batch
-  static constexpr size_t ACC_BYTES = (size_t(NACC) * 8 + 127) & ~size_t(127);
-  static constexpr size_t SMEM = ACC_BYTES + size_t(NB) * (16 + 8 + 8 * L + 4 * 3 * L + 4 * L * L);
-  static_assert(PITCH <= 128 && P1 <= 256 && P2 <= 256, "TMA box extents");
-};
-
-// The grid region of a tile's padded box lies inside the grid (no wrap):
-// the box is added with one bulk tensor reduction.
-template <int BX, int BY, int BZ>
-__device__ __forceinline__ bool tile3_interior(const Geom<float>& G, int o0, int o1, int o2) {
-  using TC = Tile3<BX, BY, BZ>;
-  const int x = o0 - 4, y = o1 - 3, z = o2 - 3;
-  return x >= 0 && y >= 0 && z >= 0 && x + TC::PITCH <= G.Nt[0] && y + TC::P1 <= G.Nt[1] && z + TC::P2 <= G.Nt[2];
-}
 
 template <int BX, int BY, int BZ, bool TABLE>
 __global__ void __launch_bounds__(256) spread_tile3_kernel(const __grid_constant__ CUtensorMap tmap, int use_tma,
@@ -172,7 +147,9 @@ __global__ void __launch_bounds__(256) spread_tile3_kernel(const __grid_constant
   asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
   __syncthreads();
 
-  if (use_tma && tile3_interior<BX, BY, BZ>(G, o0, o1, o2)) {
+  // (the bulk copy's shared-memory source must be 128-byte aligned)
+  if (use_tma && tile3_interior<BX, BY, BZ>(G, o0, o1, o2) &&
+      (static_cast<unsigned>(__cvta_generic_to_shared(acc)) & 127u) == 0) {
     if (threadIdx.x == 0) {
       const int x = 2 * (o0 - 4), y = o1 - 3, z = o2 - 3;  // x in floats: a multiple of 4 (16 bytes)
       const unsigned src = static_cast<unsigned>(__cvta_generic_to_shared(acc));
