@@ -123,6 +123,8 @@ int apply_block_size(nfft_plan* p, const int64_t* bs, const void* k, int ny) {
   }
   p->ntiles_total = nt;
   p->spread_layout = layout;
+  int rc = update_center(p);  // the grid shift is a whole number of tiles
+  if (rc) return rc;
   p->spread_pitch = spread_pitch_for(p->D, p->m, int(p->bs[0]) + 2 * p->m - 1,
                                      int((p->prm.compensated ? 4 : 2) * p->real_size), p->spread_layout == 2 ? 2 : 1);
   p->gather_pitch = spread_pitch_for(p->D == 2 ? 3 : p->D, p->m, int(p->bs[0]) + 2 * p->m - 1,

@@ -88,7 +88,7 @@ template <typename T> Grid3<T> make_grid3(const nfft_plan* p) {
   G.Nt0 = int(p->Nt[0]);
   G.Nt1 = int(p->Nt[1]);
   G.Nt2 = int(p->Nt[2]);
-  const T* inv = static_cast<const T*>(p->inv);
+  const T* inv = static_cast<const T*>(p->cur_center ? p->inv_c : p->inv);
   G.inv0 = inv;
   // singleton dimensions read the "one" entry stored after the real factors
   const T* one = inv + (p->N[0] + (p->D > 1 ? p->N[1] : 0) + (p->D > 2 ? p->N[2] : 0));

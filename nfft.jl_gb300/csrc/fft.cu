@@ -831,7 +831,7 @@ FftGeom make_fft_geom(const nfft_plan* p) {
 }
 
 template <typename T> Inv3<T> make_inv3(const nfft_plan* p) {
-  const T* inv = static_cast<const T*>(p->inv);
+  const T* inv = static_cast<const T*>(p->cur_center ? p->inv_c : p->inv);
   const T* one = inv + (p->N[0] + (p->D > 1 ? p->N[1] : 0) + (p->D > 2 ? p->N[2] : 0));
   Inv3<T> I;
   I.d[0] = inv;

@@ -107,7 +107,7 @@ __global__ void __launch_bounds__(kGradThreads) grad_nodes_kernel(Geom<T> G, Nod
     }
     const int4 nd = Nd.node4[i];
     const int t[3] = {nd.x, nd.y, nd.z};
-    const int gx = G.small_grid ? wrap_any(t[0] - m + 1 + ix, G.Nt[0]) : wrap_once(t[0] - m + 1 + ix, G.Nt[0]);
+    const int gx = G.small_grid ? wrap_any(t[0] + G.sh[0] - m + 1 + ix, G.Nt[0]) : wrap_once(t[0] + G.sh[0] - m + 1 + ix, G.Nt[0]);
     const T wx = wsel<L, D>(W0, W1, ix), dwx = wsel<L, D>(V0, V1, ix);
     T sr[D], si[D];
 #pragma unroll
@@ -124,7 +124,7 @@ __global__ void __launch_bounds__(kGradThreads) grad_nodes_kernel(Geom<T> G, Nod
         const int iy = s * RY + ry;
         const bool ok = xact && iy < L;
         const int iyc = ok ? iy : 0;
-        const int gy = G.small_grid ? wrap_any(t[1] - m + 1 + iyc, G.Nt[1]) : wrap_once(t[1] - m + 1 + iyc, G.Nt[1]);
+        const int gy = G.small_grid ? wrap_any(t[1] + G.sh[1] - m + 1 + iyc, G.Nt[1]) : wrap_once(t[1] + G.sh[1] - m + 1 + iyc, G.Nt[1]);
         const int64_t row = int64_t(gy) * G.Nt[0] + gx;
         // shuffles run on every lane; inactive rows are zeroed afterwards
         const T wy_all = wsel<L, D>(W0, W1, L + iyc);
@@ -139,7 +139,7 @@ __global__ void __launch_bounds__(kGradThreads) grad_nodes_kernel(Geom<T> G, Nod
         } else {
           for (int iz = 0; iz < L; ++iz) {
             const T wz = wsel<L, D>(W0, W1, 2 * L + iz), dwz = wsel<L, D>(V0, V1, 2 * L + iz);
-            const int gz = G.small_grid ? wrap_any(t[2] - m + 1 + iz, G.Nt[2]) : wrap_once(t[2] - m + 1 + iz, G.Nt[2]);
+            const int gz = G.small_grid ? wrap_any(t[2] + G.sh[2] - m + 1 + iz, G.Nt[2]) : wrap_once(t[2] + G.sh[2] - m + 1 + iz, G.Nt[2]);
             C v = g[int64_t(gz) * G.plane + row];
             const T a = dwx * wy * wz, b = wx * dwy * wz, c = wx * wy * dwz;
             sr[0] += a * v.x; si[0] += a * v.y;

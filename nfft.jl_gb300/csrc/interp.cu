@@ -68,7 +68,8 @@ __global__ void __launch_bounds__(kInterpThreads) interp_kernel(Geom<T> G, Nodes
 #pragma unroll
           for (int q = LN::DEG - 2; q >= 0; --q) w = fma(w, t, c[q]);
         }
-        const int gx = small ? wrap_any(nd.x - m + 1 + ix, G.Nt[0]) : wrap_once(nd.x - m + 1 + ix, G.Nt[0]);
+        const int gx = small ? wrap_any(nd.x + G.sh[0] - m + 1 + ix, G.Nt[0])
+                             : wrap_once(nd.x + G.sh[0] - m + 1 + ix, G.Nt[0]);
         const C v = __ldg(g + gx);
         ar = w * v.x;
         ai = w * v.y;
@@ -133,12 +134,12 @@ __global__ void __launch_bounds__(kInterpThreads) interp_tile_kernel(Geom<T> G, 
     const int rows = P1 * P2;
     int r = warp, y = r % P1, z = r / P1;
     for (; r < rows; r += nwarps) {
-      const int gy = D >= 2 ? (small ? wrap_any(o1 - m1 + y, G.Nt[1]) : wrap_once(o1 - m1 + y, G.Nt[1])) : 0;
-      const int gz = D == 3 ? (small ? wrap_any(o2 - m1 + z, G.Nt[2]) : wrap_once(o2 - m1 + z, G.Nt[2])) : 0;
+      const int gy = D >= 2 ? wrap_any(o1 + G.sh[1] - m1 + y, G.Nt[1]) : 0;
+      const int gz = D == 3 ? wrap_any(o2 + G.sh[2] - m1 + z, G.Nt[2]) : 0;
       const C* grow = g + int64_t(gz) * G.plane + int64_t(gy) * G.Nt[0];
       C* srow = tile + z * plane + y * pitch;
       for (int x = lane; x < P0; x += 32) {
-        const int gx = small ? wrap_any(o0 - m1 + x, G.Nt[0]) : wrap_once(o0 - m1 + x, G.Nt[0]);
+        const int gx = wrap_any(o0 + G.sh[0] - m1 + x, G.Nt[0]);
         cp_async_elem(srow + x, grow + gx);
       }
       y += nwarps;
@@ -295,6 +296,9 @@ __global__ void __launch_bounds__(kInterpThreads) interp_tile3_kernel(const __gr
   const int tc1 = (t / G.ntiles[0]) % G.ntiles[1];
   const int tc2 = t / (G.ntiles[0] * G.ntiles[1]);
   const int o0 = tc0 * BX, o1 = tc1 * BY, o2 = tc2 * BZ;
+  // the tile's origin in the (possibly centred) grid; a whole number of tiles
+  const int q0 = wrap_once(o0 + G.sh[0], G.Nt[0]), q1 = wrap_once(o1 + G.sh[1], G.Nt[1]);
+  const int q2 = wrap_once(o2 + G.sh[2], G.Nt[2]);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   constexpr int NWARPS = kInterpThreads / 32;
   PolyRegs<3, 8, float> P;
@@ -302,7 +306,7 @@ __global__ void __launch_bounds__(kInterpThreads) interp_tile3_kernel(const __gr
   const unsigned tile_s = static_cast<unsigned>(__cvta_generic_to_shared(tile));
   const unsigned mbar_s = static_cast<unsigned>(__cvta_generic_to_shared(mbar));
   // the bulk copy's shared-memory destination must be 128-byte aligned
-  if (!tile3_interior<BX, BY, BZ>(G, o0, o1, o2) || (tile_s & 127u) != 0) {
+  if (!tile3_interior<BX, BY, BZ>(G, q0, q1, q2) || (tile_s & 127u) != 0) {
     for (int64_t i = task.y + warp; i < task.z; i += NWARPS) interp_node<3, 8, float, TABLE>(G, Nd, P, i, lane, g, fhat);
     return;
   }
@@ -316,7 +320,7 @@ __global__ void __launch_bounds__(kInterpThreads) interp_tile3_kernel(const __gr
     asm volatile(
         "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
         "[%5];" ::"r"(tile_s),
-        "l"(reinterpret_cast<uint64_t>(&tmap)), "r"(2 * (o0 - 4)), "r"(o1 - 3), "r"(o2 - 3), "r"(mbar_s)
+        "l"(reinterpret_cast<uint64_t>(&tmap)), "r"(2 * (q0 - 4)), "r"(q1 - 3), "r"(q2 - 3), "r"(mbar_s)
         : "memory");
   }
   bool done = false;

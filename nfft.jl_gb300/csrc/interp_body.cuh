@@ -21,7 +21,7 @@ __device__ __forceinline__ void interp_node(const Geom<T>& G, const Nodes<T>& Nd
   const int4 nd = __ldg(Nd.node4 + i);
   T W[LN::NW];
   node_weights<D, L, T, TABLE>(Nd, P, i, lane, W);
-  const int gx = small ? wrap_any(nd.x - m + 1 + ix, Nt0) : wrap_once(nd.x - m + 1 + ix, Nt0);
+  const int gx = small ? wrap_any(nd.x + G.sh[0] - m + 1 + ix, Nt0) : wrap_once(nd.x + G.sh[0] - m + 1 + ix, Nt0);
   const T wx = wsel<D, L>(W, ix);
   int row[LN::NSTEP];
   T wxy[LN::NSTEP];
@@ -30,7 +30,7 @@ __device__ __forceinline__ void interp_node(const Geom<T>& G, const Nodes<T>& Nd
     const int iy = s * LN::RY + ry;
     const bool ok = xact && iy < L;
     const int iyc = ok ? iy : 0;
-    const int gy = small ? wrap_any(nd.y - m + 1 + iyc, Nt1) : wrap_once(nd.y - m + 1 + iyc, Nt1);
+    const int gy = small ? wrap_any(nd.y + G.sh[1] - m + 1 + iyc, Nt1) : wrap_once(nd.y + G.sh[1] - m + 1 + iyc, Nt1);
     row[s] = gy * Nt0 + gx;
     const T wy = wsel<D, L>(W, L + iyc);  // every lane shuffles
     wxy[s] = ok ? wx * wy : T(0);
@@ -48,7 +48,8 @@ __device__ __forceinline__ void interp_node(const Geom<T>& G, const Nodes<T>& Nd
     C v[L][LN::NSTEP];
 #pragma unroll
     for (int iz = 0; iz < L; ++iz) {
-      const int gz = small ? wrap_any(nd.z - m + 1 + iz, G.Nt[2]) : wrap_once(nd.z - m + 1 + iz, G.Nt[2]);
+      const int gz = small ? wrap_any(nd.z + G.sh[2] - m + 1 + iz, G.Nt[2])
+                           : wrap_once(nd.z + G.sh[2] - m + 1 + iz, G.Nt[2]);
       const C* gp = g + int64_t(gz) * G.plane;
 #pragma unroll
       for (int s = 0; s < LN::NSTEP; ++s) v[iz][s] = __ldg(gp + row[s]);

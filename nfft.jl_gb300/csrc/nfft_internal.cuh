@@ -64,6 +64,7 @@ template <typename T> struct Geom {
   const T* coeffs;        // (2m+1) x 2m, column l contiguous (POLY)
   const T* lut;           // LUTSize+2 (LINEAR)
   bool small_grid;        // some Ntilde < 2m: taps may wrap more than once
+  int sh[kMaxDim];        // grid position of index n is (n + sh) mod Ntilde (the centred internal grid; else 0)
 };
 
 // Sorted node data produced by nfft_set_nodes.
@@ -114,6 +115,17 @@ struct nfft_plan {
 
   void* grid = nullptr;       // tmpVec, |Ntilde| complex
   void* inv = nullptr;        // deconvolution factors, N0+N1+N2 reals
+  // Centred internal grid: the forward / adjoint transforms keep the
+  // oversampled grid shifted by sh = Ntilde/2 in every dimension where that is
+  // a whole number of tiles (an fftshift), so the dense centre of k-space (grid
+  // index 0) lies inside the grid instead of at its corner.  The shift is the
+  // factor (-1)^k on the grid frequencies, folded into inv_c = inv times
+  // (-1)^(n - N/2); convolve!/deconvolve! and the batched and directional
+  // paths keep the reference layout (cur_center = 0).
+  bool center = true;
+  int64_t sh[3] = {0, 0, 0};
+  void* inv_c = nullptr;
+  int cur_center = 0;
   void* coeffs = nullptr;     // poly coefficients (T)
   void* lut = nullptr;        // LINEAR lut (T)
   double coeffs_host[nfft::kMaxDeg * nfft::kMaxL] = {};
@@ -213,6 +225,14 @@ int launch_plain_interp(const nfft_plan* p, const void* g, int g_real, void* fha
 int launch_plain_spread(const nfft_plan* p, const void* fhat, int fhat_real, void* g, int g_real);
 
 template <typename T> Geom<T> make_geom(const nfft_plan* p);
+// plan.cu: recompute sh and inv_c after the tiles or the factors changed
+int update_center(nfft_plan* p);
+// the centred grid during one forward / adjoint / gradient call
+struct CenterScope {
+  nfft_plan* p;
+  explicit CenterScope(nfft_plan* q) : p(q) { p->cur_center = (p->sh[0] | p->sh[1] | p->sh[2]) != 0; }
+  ~CenterScope() { p->cur_center = 0; }
+};
 template <typename T> Nodes<T> make_nodes(const nfft_plan* p);
 
 // ------------------------------------------------------------ device helpers

@@ -18,7 +18,7 @@ __device__ __forceinline__ void plain_setup(const Geom<T>& G, const T* cs, const
     T e;
     reduce_coord<T>(k[d + int64_t(D) * j], G.Nt[d], t, e);
     for (int l = 0; l < L; ++l) {
-      idx[d][l] = wrap_any(t - G.m + 1 + l, G.Nt[d]);
+      idx[d][l] = wrap_any(t + G.sh[d] - G.m + 1 + l, G.Nt[d]);
       w[d][l] = tap_weight<T>(G, cs, e, l);
     }
   }

@@ -45,10 +45,64 @@ template <typename T> Geom<T> make_geom(const nfft_plan* p) {
   G.coeffs = static_cast<const T*>(p->coeffs);
   G.lut = static_cast<const T*>(p->lut);
   G.small_grid = small;
+  for (int d = 0; d < kMaxDim; ++d) G.sh[d] = p->cur_center ? int(p->sh[d]) : 0;
   return G;
 }
 template Geom<float> make_geom<float>(const nfft_plan*);
 template Geom<double> make_geom<double>(const nfft_plan*);
+
+// inv_c[i] = inv[i] * (-1)^(n - N_d/2) for the factors of dimensions with a
+// grid shift (n = image index within dimension d's segment), inv[i] elsewhere.
+template <typename T>
+__global__ void centre_factors_kernel(const T* __restrict__ inv, T* __restrict__ inv_c, int64_t n, int N0, int N1,
+                                      int N2, int s0, int s1, int s2) {
+  const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  int d = -1, k = 0, Nd = 1;
+  if (i < N0) {
+    d = 0; k = int(i); Nd = N0;
+  } else if (i < N0 + N1) {
+    d = 1; k = int(i - N0); Nd = N1;
+  } else if (i < N0 + N1 + N2) {
+    d = 2; k = int(i - N0 - N1); Nd = N2;
+  }
+  const int s = d == 0 ? s0 : d == 1 ? s1 : d == 2 ? s2 : 0;
+  const T v = inv[i];
+  inv_c[i] = (s && ((k - Nd / 2) & 1)) ? -v : v;
+}
+
+int update_center(nfft_plan* p) {
+  for (int d = 0; d < 3; ++d) p->sh[d] = 0;
+  if (!p->center || !p->prm.blocking) return NFFT_OK;
+  bool any = false;
+  for (int d = 0; d < p->D; ++d) {
+    const int64_t h = p->Nt[d] / 2;
+    if (p->Nt[d] % 2 == 0 && h > 0 && h % p->bs[d] == 0) {
+      p->sh[d] = h;
+      any = true;
+    }
+  }
+  if (!any) return NFFT_OK;
+  const int N0 = int(p->N[0]), N1 = p->D > 1 ? int(p->N[1]) : 0, N2 = p->D > 2 ? int(p->N[2]) : 0;
+  const int64_t ninv = int64_t(N0) + N1 + N2 + 1;
+  if (!p->inv_c && cudaMalloc(&p->inv_c, p->real_size * size_t(ninv)) != cudaSuccess) {
+    p->inv_c = nullptr;
+    for (int d = 0; d < 3; ++d) p->sh[d] = 0;
+    set_error("cudaMalloc of the centred deconvolution factors failed");
+    return NFFT_ERR_ALLOC;
+  }
+  const unsigned nb = unsigned((ninv + 255) / 256);
+  if (p->precision == 32)
+    centre_factors_kernel<float><<<nb, 256, 0, p->stream>>>(static_cast<const float*>(p->inv),
+                                                             static_cast<float*>(p->inv_c), ninv, N0, N1, N2,
+                                                             p->sh[0] != 0, p->sh[1] != 0, p->sh[2] != 0);
+  else
+    centre_factors_kernel<double><<<nb, 256, 0, p->stream>>>(static_cast<const double*>(p->inv),
+                                                              static_cast<double*>(p->inv_c), ninv, N0, N1, N2,
+                                                              p->sh[0] != 0, p->sh[1] != 0, p->sh[2] != 0);
+  NFFT_LAUNCH_CHECK();
+  return NFFT_OK;
+}
 
 template <typename T> Nodes<T> make_nodes(const nfft_plan* p) {
   Nodes<T> n{};
@@ -480,6 +534,8 @@ int nfft_plan_create(nfft_plan** out, int precision, int D, const int64_t* N, in
   if (const char* e = getenv("NFFT_GB300_SPREAD_TILE3")) p->spread_tile3 = e[0] != '0';
   if (const char* e = getenv("NFFT_GB300_SPREAD_TMA")) p->spread_tma = e[0] != '0';
   if (const char* e = getenv("NFFT_GB300_GATHER_TMA")) p->gather_tma = e[0] != '0';
+  // the centred internal grid of the transforms (on by default)
+  if (const char* e = getenv("NFFT_GB300_CENTER")) p->center = e[0] != '0';
   p->ntiles_total = 1;
   for (int d = 0; d < 3; ++d) {
     p->ntiles[d] = (p->Nt[d] + p->bs[d] - 1) / p->bs[d];
@@ -545,6 +601,8 @@ int nfft_plan_create(nfft_plan** out, int precision, int D, const int64_t* N, in
   }
   int rc = launch_deconv_factors(p);
   if (rc) return fail(rc);
+  rc = update_center(p);
+  if (rc) return fail(rc);
   // cuFFT plans (Julia's column-major grid is C order with reversed dims)
   rc = make_fft_plans(p);
   if (rc) return fail(rc);
@@ -570,6 +628,7 @@ int nfft_plan_destroy(nfft_plan* p) {
   free_nodes(p);
   cudaFree(p->grid);
   cudaFree(p->inv);
+  cudaFree(p->inv_c);
   cudaFree(p->coeffs);
   cudaFree(p->lut);
   cudaFree(p->dflag);
@@ -724,6 +783,7 @@ static int require_nodes(const nfft_plan* p) {
 int nfft_forward(nfft_plan* p, const void* f, void* fhat) {
   int rc = require_nodes(p);
   if (rc) return rc;
+  CenterScope centred(p);
   const int slot = p->timing_on ? ring_slot(p) : 0;
   record(p, slot, 0);
   rc = p->fused_fft ? fused_forward_x(p, f) : launch_pad_apodize(p, f, p->grid);
@@ -742,6 +802,7 @@ int nfft_forward(nfft_plan* p, const void* f, void* fhat) {
 int nfft_adjoint(nfft_plan* p, const void* fhat, void* f) {
   int rc = require_nodes(p);
   if (rc) return rc;
+  CenterScope centred(p);
   const int slot = p->timing_on ? ring_slot(p) : 0;
   record(p, slot, 0);
   rc = p->prm.blocking ? launch_spread(p, fhat, 0, p->grid, 0) : launch_plain_spread(p, fhat, 0, p->grid, 0);
@@ -824,6 +885,7 @@ int nfft_deconvolve_transpose(nfft_plan* p, const void* g, void* f) {
 int nfft_grad_nodes(nfft_plan* p, const void* v, const void* w, void* dk) {
   int rc = require_nodes(p);
   if (rc) return rc;
+  CenterScope centred(p);
   rc = p->fused_fft ? fused_forward_x(p, v) : launch_pad_apodize(p, v, p->grid);
   if (rc) return rc;
   rc = p->fused_fft ? fused_forward_lines(p) : exec_fft(p, CUFFT_FORWARD);

@@ -57,7 +57,7 @@ __device__ __forceinline__ void flush_tile(const Geom<T>& G, const typename Acc<
   const int m1 = G.m - 1;
   const bool small = G.small_grid;
   const int Nt0 = G.Nt[0];
-  const int x0 = o0 - m1;                                  // grid x of padded column 0
+  const int x0 = o0 + G.sh[0] - m1;                        // grid x of padded column 0
   const int lead = pair ? (x0 & 1) : 0;                    // column 0 is the odd half of a pair
   const int nunit = pair ? (P0 + lead + 1) >> 1 : P0;      // units per row
   const int lpr = nunit < 32 ? nunit : 32;                 // lanes per row
@@ -69,8 +69,10 @@ __device__ __forceinline__ void flush_tile(const Geom<T>& G, const typename Acc<
   int r = rr < rpi ? warp * rpi + rr : rows;
   int y = r % P1, z = r / P1;
   for (; r < rows; r += step) {
-    const int gy = D >= 2 ? (small ? wrap_any(o1 - m1 + y, G.Nt[1]) : wrap_once(o1 - m1 + y, G.Nt[1])) : 0;
-    const int gz = D == 3 ? (small ? wrap_any(o2 - m1 + z, G.Nt[2]) : wrap_once(o2 - m1 + z, G.Nt[2])) : 0;
+    const int gy = D >= 2 ? (small ? wrap_any(o1 + G.sh[1] - m1 + y, G.Nt[1]) : wrap_once(o1 + G.sh[1] - m1 + y, G.Nt[1]))
+                          : 0;
+    const int gz = D == 3 ? (small ? wrap_any(o2 + G.sh[2] - m1 + z, G.Nt[2]) : wrap_once(o2 + G.sh[2] - m1 + z, G.Nt[2]))
+                          : 0;
     T* grow = g + 2 * (int64_t(gz) * G.plane + int64_t(gy) * Nt0);
     const auto* srow = acc + z * plane + y * pitch;
     for (int j = j0; j < nunit; j += lpr) {
@@ -444,7 +446,7 @@ __global__ void __launch_bounds__(kSpreadThreads) spread_pad1_kernel(Geom<T> G, 
   for (int x = threadIdx.x; x < P0; x += blockDim.x) {
     const T a = sre[x], bb = sim[x];
     if (a != T(0) || bb != T(0)) {
-      const int gx = small ? wrap_any(o0 - m1 + x, G.Nt[0]) : wrap_once(o0 - m1 + x, G.Nt[0]);
+      const int gx = small ? wrap_any(o0 + G.sh[0] - m1 + x, G.Nt[0]) : wrap_once(o0 + G.sh[0] - m1 + x, G.Nt[0]);
       red_add2<T>(g + 2 * int64_t(gx), a, bb);
     }
   }

@@ -148,10 +148,13 @@ __global__ void __launch_bounds__(256) spread_tile3_kernel(const __grid_constant
   __syncthreads();
 
   // (the bulk copy's shared-memory source must be 128-byte aligned)
-  if (use_tma && tile3_interior<BX, BY, BZ>(G, o0, o1, o2) &&
+  // the tile's origin in the (possibly centred) grid; a whole number of tiles
+  const int q0 = wrap_once(o0 + G.sh[0], G.Nt[0]), q1 = wrap_once(o1 + G.sh[1], G.Nt[1]);
+  const int q2 = wrap_once(o2 + G.sh[2], G.Nt[2]);
+  if (use_tma && tile3_interior<BX, BY, BZ>(G, q0, q1, q2) &&
       (static_cast<unsigned>(__cvta_generic_to_shared(acc)) & 127u) == 0) {
     if (threadIdx.x == 0) {
-      const int x = 2 * (o0 - 4), y = o1 - 3, z = o2 - 3;  // x in floats: a multiple of 4 (16 bytes)
+      const int x = 2 * (q0 - 4), y = q1 - 3, z = q2 - 3;  // x in floats: a multiple of 4 (16 bytes)
       const unsigned src = static_cast<unsigned>(__cvta_generic_to_shared(acc));
       asm volatile(
           "cp.reduce.async.bulk.tensor.3d.global.shared::cta.add.tile.bulk_group [%0, {%1, %2, %3}], [%4];"
