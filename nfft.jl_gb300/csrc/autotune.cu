@@ -176,6 +176,7 @@ extern "C" int nfft_autotune(nfft_plan* p, int use_cache) {
   std::vector<int64_t> best_bs = {p->bs[0], p->bs[1], p->bs[2], p->spread_layout};
   for (const auto& c : candidates(p)) {
     if (apply_block_size(p, c.data(), k, int(c[3])) != NFFT_OK) continue;
+    CenterScope centred(p);  // time the grid layout the transforms use
     float times[3];
     bool ok = true;
     for (int r = 0; r < 3 && ok; ++r) {

@@ -310,6 +310,15 @@ __global__ void __launch_bounds__(kInterpThreads) interp_tile3_kernel(const __gr
     for (int64_t i = task.y + warp; i < task.z; i += NWARPS) interp_node<3, 8, float, TABLE>(G, Nd, P, i, lane, g, fhat);
     return;
   }
+  // the first node's record and window values are loaded while the tile arrives
+  const int ix = lane & 7, ry = lane >> 3;
+  int64_t i = task.y + warp;
+  int4 nd = make_int4(0, 0, 0, 0);
+  float W[LN::NW];
+  if (i < task.z) {
+    nd = __ldg(Nd.node4 + i);
+    node_weights<3, 8, float, TABLE>(Nd, P, i, lane, W);
+  }
   if (threadIdx.x == 0) {
     mbar_init(mbar_s, 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -329,11 +338,15 @@ __global__ void __launch_bounds__(kInterpThreads) interp_tile3_kernel(const __gr
     if (threadIdx.x == 0) atomicOr(status, 1);
     return;
   }
-  const int ix = lane & 7, ry = lane >> 3;
-  for (int64_t i = task.y + warp; i < task.z; i += NWARPS) {
-    const int4 nd = __ldg(Nd.node4 + i);
-    float W[LN::NW];
-    node_weights<3, 8, float, TABLE>(Nd, P, i, lane, W);
+  for (; i < task.z; i += NWARPS) {
+    // software pipeline: the next node's global loads are issued before this node's sums
+    const int64_t in = i + NWARPS;
+    int4 ndn = nd;
+    float Wn[LN::NW];
+    if (in < task.z) {
+      ndn = __ldg(Nd.node4 + in);
+      node_weights<3, 8, float, TABLE>(Nd, P, in, lane, Wn);
+    }
     const float wx = wsel<3, 8>(W, ix);
     const float wy0 = wsel<3, 8>(W, 8 + ry), wy1 = wsel<3, 8>(W, 12 + ry);
     const float2* base = tile + (nd.z - o2) * PLANE + (nd.y - o1 + ry) * PITCH + (nd.x - o0 + 1) + ix;
@@ -360,6 +373,9 @@ __global__ void __launch_bounds__(kInterpThreads) interp_tile3_kernel(const __gr
       ai += __shfl_xor_sync(0xFFFFFFFFu, ai, o);
     }
     if (lane == 0) fhat[nd.w] = make_float2(ar, ai);
+    nd = ndn;
+#pragma unroll
+    for (int r = 0; r < LN::NW; ++r) W[r] = Wn[r];
   }
 }
 
