@@ -42,17 +42,27 @@ N3 = (256, 256, 256)
 SPOKES, SAMPLES = 8192, 512
 M_NODES = SPOKES * SAMPLES
 WORKLOAD = "3D radial koosh-ball NFFT fwd+adj, N=256^3, 8192 spokes x 512 samples (M=4194304), KB m=4 sigma=2"
-# DRAM bytes (read + write) per launch of the spreading kernel on this
-# workload, from one ncu capture of the full-size launch
-# (profiles/spread_owned_radial256.md: 1.115 GB read + 0.564 GB write).
-SPREAD_DRAM_BYTES = 1.679e9
-# What bounds the dominant kernel on chip (same capture).
+# The workload's configuration, identical in both arms (the GPU arm's tile
+# shape and the like go to the line's "run" object).
+def config_dict(**kw):
+    cfg = {"workload": WORKLOAD, "precision": "FP32", "precompute": "TENSOR",
+           "window": "kaiser_bessel, m=4, sigma=2",
+           "l2": "inputs larger than L2 (grid 1.07 GB, image 134 MB); no extra flush"}
+    cfg.update(kw)
+    return cfg
+# DRAM bytes (read + write) per launch of the dominant kernel on this workload,
+# from one ncu capture (dram__bytes_read.sum + dram__bytes_write.sum, one
+# launch, tiles 16x8x8): 1.17 GB read + 0.602 GB write.  Not measured in the
+# run itself; the line says so.
+SPREAD_DRAM_BYTES = 1.774e9
+SPREAD_TRAFFIC_SOURCE = "ncu capture of spread_tile3_kernel on this workload (one launch), not measured in this run"
 # DRAM bytes (read + write) of one Toeplitz application at 256^3 (the five
-# kernels of the fused path), from the ncu launch list of the profiling case
-# (profiles/toeplitz_apply_256.md: 2.821 GB read + 1.049 GB write).
+# kernels of the fused path), from an ncu capture of the profiling case:
+# 2.821 GB read + 1.049 GB write.
 TOEPLITZ_DRAM_BYTES = 3.870e9
-SPREAD_LIMITER = ("shared-memory pipe 73.3% and instruction issue 81.6% of peak (ncu); the 20 B of shared-memory "
-                  "traffic per tap put the tap phase at 1.07 ms, HBM is not the limiter")
+SPREAD_LIMITER = ("shared-memory wavefronts ~65% and instruction issue ~60% of peak (ncu, 128^3 case): the "
+                  "read-modify-write of the padded tile in shared memory (16 B per tap; 512 taps per node) "
+                  "bounds the kernel, HBM is not the limiter (DRAM throughput ~6%)")
 
 
 def radial_nodes(dtype=np.float32):
@@ -269,6 +279,12 @@ def cpu_reference_run(steps, warmup, budget_s=150.0):
                       f"oracle restatement of NFFT.jl blocked TENSOR, FFT via scipy.fft workers={threads}"}
 
 
+def oracle_block_size():
+    """The reference's _blockSize for the workload's oversampled grid."""
+    from oracle import oracle
+    return oracle.default_block_size(tuple(2 * n for n in N3))
+
+
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -278,7 +294,8 @@ def run_reference(args):
         "impl": "reference", "metric": METRIC, "value": r["value"], "unit": UNIT, "n_gpus": args.gpus,
         "steps": r["steps"], "warmup": r["warmup"], "ms_per_step": r["seconds_per_step"] * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "precision": "FP32", "parallelism": "host threads"},
+        "config": config_dict(),
+        "run": {"parallelism": "host threads", "block_size": list(oracle_block_size())},
         "cpu_baseline": {"value": r["value"], "unit": UNIT, "cores": r["cores"], "kind": "port",
                          "sample": r["sample"]},
         "e2e": {"value": r["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -470,13 +487,14 @@ def run_ours(args):
     dom = max(alg, key=lambda s: stages[s])
     t_dom = stages[dom] * 1e-3
     achieved = alg[dom] / t_dom / 1e9
-    kernel_names = {"spread_ms": "spread_owned_kernel (stage: grid memset + value sort + kernel)",
-                    "gather_ms": "interp_kernel", "deconv_pad_ms": "fft_x_pad_kernel",
-                    "crop_ms": "fft_x_crop_kernel"}
+    kernel_names = {"spread_ms": "spread_tile3_kernel (stage: grid memset + value sort + kernel)",
+                    "gather_ms": "interp_tile3_kernel", "deconv_pad_ms": "fft4_x_kernel (forward)",
+                    "crop_ms": "fft4_x_kernel (adjoint)"}
     roofline = {"bound": "hbm", "kernel": kernel_names[dom], "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "peak_source": f"{peak_kind} hbm_gbs",
                 "algorithmic_bytes": alg[dom],
                 "traffic": SPREAD_DRAM_BYTES if dom == "spread_ms" else None,
+                "traffic_source": SPREAD_TRAFFIC_SOURCE if dom == "spread_ms" else None,
                 "limiter": SPREAD_LIMITER if dom == "spread_ms" else None}
     pair_bytes = 7 * ng * s_c + 3 * nimg * s_c + 2 * M_NODES * (D * s_r + s_c)
     pair_gbs = pair_bytes / (t_dev / args.steps) / 1e9
@@ -491,12 +509,11 @@ def run_ours(args):
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": t_dev / args.steps * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "precision": "FP32 (FP64 node reduction and deconvolution factors)",
-                       "precompute": args.precompute.upper(),
-                       "block_size": list(p.params.blockSize),
-                       "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
-                       "l2": "inputs larger than L2 (grid 1.07 GB, image 134 MB); no extra flush",
-                       "plan_seconds": t_pre},
+            "config": config_dict(precompute=args.precompute.upper()),
+            "run": {"block_size": list(p.params.blockSize),
+                    "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
+                    "precision_detail": "FP32 data and sums; FP64 node reduction and deconvolution factors",
+                    "plan_seconds": t_pre},
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                     "steps": e2e_steps,
                     "copies": "pinned host <-> device every step on two copy streams, three buffer sets, "
@@ -672,6 +689,22 @@ def run_config(args):
     l0 = nf.kernel_launch_count()
     t_ours = timed(step, args.steps, args.warmup)
     launches = (nf.kernel_launch_count() - l0) // (args.steps + args.warmup)
+    rebin = None
+    if grad:
+        # a node-optimisation step moves the nodes: nodes! (check, binning,
+        # window tensor, tasks) precedes fwd + adj + dk every step, as
+        # nfftgb300.autodiff.nfft_nodes does on every call
+        kd = torch.as_tensor(k).to(dev)
+
+        def step_rebin():
+            p.nodes_(kd)
+            step()
+
+        t_rb = timed(step_rebin, args.steps, args.warmup)
+        rebin = {"value": M / t_rb, "unit": UNIT, "ms_per_step": t_rb * 1e3,
+                 "nodes_ms": (t_rb - t_ours) * 1e3,
+                 "what": "each step re-bins the nodes (nodes!) before fwd + adj + dk, as a node-optimisation "
+                         "step does"}
     yo, xo = y.cpu().numpy(), x.cpu().numpy()
     k64 = k.astype(np.float64)
     err = rel_err_subset(k64, f_h, fh_h, yo, xo)
@@ -680,6 +713,8 @@ def run_config(args):
             "ms_per_step": t_ours * 1e3, "higher_is_better": True, "dtype": "f32" if cfg["prec"] == 32 else "f64",
             "data": "synthetic", "config": {"workload": cfg["desc"], "block_size": list(p.params.blockSize)},
             "gpu_launches_per_step": launches, "rel_err_vs_fp64_ndft": err}
+    if rebin is not None:
+        line["with_rebinning"] = rebin
     # the reference's GPU algorithm (sparse B), where it fits
     if not args.no_plain and M * (2 * m) ** len(N) < 2 ** 31:
         inv = np.concatenate([p.deconv_factors()[d] for d in range(len(N))])
