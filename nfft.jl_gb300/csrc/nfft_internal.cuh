@@ -153,6 +153,13 @@ struct nfft_plan {
   int64_t tmap_key = 0;
   int gather_pitch = 0;            // shared-memory row pitch of the staged gather tile
   bool gather_tiled = false;       // gather from shared-memory tiles (else straight from L1/L2)
+  // device buffers of nfft_set_nodes, kept across calls (nodes! every step of
+  // a node optimisation) and grown on demand; the node tables above point
+  // into the first ones
+  enum { NB_K, NB_NODE4, NB_FRAC4, NB_WTAB, NB_TSTART, NB_TASKS, NB_FSORTED, NB_TI, NB_TE, NB_KEY, NB_VAL,
+         NB_KEY2, NB_VAL2, NB_TCOUNT, NB_SCR, NB_TCNT, NB_TOFF, NB_COUNT };
+  void* nbuf[NB_COUNT] = {};
+  size_t nbuf_cap[NB_COUNT] = {};
   int* dflag = nullptr;            // device status words: [0] node check, [1] an async copy wait that timed out
   size_t scratch_bytes = 0;
 
@@ -225,6 +232,8 @@ int launch_plain_interp(const nfft_plan* p, const void* g, int g_real, void* fha
 int launch_plain_spread(const nfft_plan* p, const void* fhat, int fhat_real, void* g, int g_real);
 
 template <typename T> Geom<T> make_geom(const nfft_plan* p);
+// plan.cu: node buffer `which` of at least `bytes` (grown, contents not kept)
+void* node_buffer(nfft_plan* p, int which, size_t bytes);
 // plan.cu: recompute sh and inv_c after the tiles or the factors changed
 int update_center(nfft_plan* p);
 // the centred grid during one forward / adjoint / gradient call

@@ -71,6 +71,24 @@ __global__ void centre_factors_kernel(const T* __restrict__ inv, T* __restrict__
   inv_c[i] = (s && ((k - Nd / 2) & 1)) ? -v : v;
 }
 
+void* node_buffer(nfft_plan* p, int which, size_t bytes) {
+  if (bytes == 0) bytes = 16;
+  if (p->nbuf_cap[which] < bytes) {
+    cudaFree(p->nbuf[which]);
+    p->nbuf[which] = nullptr;
+    p->nbuf_cap[which] = 0;
+    // 1/8 headroom: node sets that grow a little do not reallocate every time
+    const size_t want = bytes + bytes / 8;
+    if (cudaMalloc(&p->nbuf[which], want) != cudaSuccess) {
+      p->nbuf[which] = nullptr;
+      set_error("cudaMalloc of %zu bytes of node buffers failed", want);
+      return nullptr;
+    }
+    p->nbuf_cap[which] = want;
+  }
+  return p->nbuf[which];
+}
+
 int update_center(nfft_plan* p) {
   for (int d = 0; d < 3; ++d) p->sh[d] = 0;
   if (!p->center || !p->prm.blocking) return NFFT_OK;
@@ -224,21 +242,25 @@ void default_block(nfft_plan* p) {
   }
 }
 
+// The plan forgets its nodes; the node buffers stay allocated for the next
+// nfft_set_nodes.
 void free_nodes(nfft_plan* p) {
-  cudaFree(p->k);
-  cudaFree(p->node4);
-  cudaFree(p->frac4);
-  cudaFree(p->wtab);
-  cudaFree(p->tile_start);
-  cudaFree(p->tasks);
-  cudaFree(p->fsorted);
-  p->fsorted = nullptr;
   p->k = p->frac4 = p->wtab = nullptr;
+  p->fsorted = nullptr;
   p->node4 = nullptr;
   p->tile_start = nullptr;
   p->tasks = nullptr;
   p->n_tasks = 0;
   p->has_nodes = false;
+}
+
+void release_node_buffers(nfft_plan* p) {
+  free_nodes(p);
+  for (int i = 0; i < nfft_plan::NB_COUNT; ++i) {
+    cudaFree(p->nbuf[i]);
+    p->nbuf[i] = nullptr;
+    p->nbuf_cap[i] = 0;
+  }
 }
 
 int bits_for(int64_t n) {
@@ -625,7 +647,7 @@ int nfft_plan_create(nfft_plan** out, int precision, int D, const int64_t* N, in
 
 int nfft_plan_destroy(nfft_plan* p) {
   if (!p) return NFFT_OK;
-  free_nodes(p);
+  release_node_buffers(p);
   cudaFree(p->grid);
   cudaFree(p->inv);
   cudaFree(p->inv_c);
@@ -666,13 +688,14 @@ int nfft_set_nodes(nfft_plan* p, const void* k, int k_on_device) {
   cudaStream_t s = p->stream;
   const int L = 2 * p->m;
   const bool table = p->prm.precompute != NFFT_PRECOMPUTE_POLYNOMIAL;
-  if (cudaMalloc(&p->k, rs * size_t(D * M > 0 ? D * M : 1)) != cudaSuccess ||
-      cudaMalloc(&p->node4, sizeof(int4) * size_t(M > 0 ? M : 1)) != cudaSuccess ||
-      cudaMalloc(&p->frac4, rs * 4 * size_t(M > 0 ? M : 1)) != cudaSuccess ||
-      (table && cudaMalloc(&p->wtab, rs * size_t(M > 0 ? M * D * L : 1)) != cudaSuccess) ||
-      cudaMalloc(&p->tile_start, sizeof(int32_t) * size_t(p->ntiles_total + 1)) != cudaSuccess) {
+  using P = nfft_plan;
+  p->k = node_buffer(p, P::NB_K, rs * size_t(D * M));
+  p->node4 = static_cast<int4*>(node_buffer(p, P::NB_NODE4, sizeof(int4) * size_t(M)));
+  p->frac4 = node_buffer(p, P::NB_FRAC4, rs * 4 * size_t(M));
+  p->wtab = table ? node_buffer(p, P::NB_WTAB, rs * size_t(M * D * L)) : nullptr;
+  p->tile_start = static_cast<int32_t*>(node_buffer(p, P::NB_TSTART, sizeof(int32_t) * size_t(p->ntiles_total + 1)));
+  if (!p->k || !p->node4 || !p->frac4 || (table && !p->wtab) || !p->tile_start) {
     free_nodes(p);
-    set_error("cudaMalloc of node arrays failed");
     return NFFT_ERR_ALLOC;
   }
   if (M > 0) {
@@ -694,31 +717,31 @@ int nfft_set_nodes(nfft_plan* p, const void* k, int k_on_device) {
   const int64_t nt = p->ntiles_total;
   const int kbits = bits_for(nt);
   {
-    // reduce + stable radix sort by home tile
-    DevBuf ti_u, te_u, key, val, key2, val2, tcount, scr;
-    NFFT_ALLOC(ti_u, sizeof(int32_t) * size_t(D * M));
-    NFFT_ALLOC(te_u, rs * size_t(D * M));
-    NFFT_ALLOC(key, sizeof(uint32_t) * size_t(M));
-    NFFT_ALLOC(val, sizeof(int32_t) * size_t(M));
-    NFFT_ALLOC(key2, sizeof(uint32_t) * size_t(M));
-    NFFT_ALLOC(val2, sizeof(int32_t) * size_t(M));
-    NFFT_ALLOC(tcount, sizeof(int32_t) * size_t(nt + 1));
+    // reduce + stable radix sort by home tile (scratch kept on the plan)
     const size_t sb = std::max(radix_sort_scratch_bytes(M), scan_scratch_bytes(nt + 1));
-    NFFT_ALLOC(scr, sb);
-    NFFT_CUDA_TRY(cudaMemsetAsync(tcount.p, 0, sizeof(int32_t) * size_t(nt + 1), s));
-    rc = launch_reduce_nodes(p, p->k, static_cast<int32_t*>(ti_u.p), te_u.p, static_cast<uint32_t*>(key.p),
-                             static_cast<int32_t*>(val.p), static_cast<int32_t*>(tcount.p));
+    auto* ti_u = static_cast<int32_t*>(node_buffer(p, P::NB_TI, sizeof(int32_t) * size_t(D * M)));
+    void* te_u = node_buffer(p, P::NB_TE, rs * size_t(D * M));
+    auto* key = static_cast<uint32_t*>(node_buffer(p, P::NB_KEY, sizeof(uint32_t) * size_t(M)));
+    auto* val = static_cast<int32_t*>(node_buffer(p, P::NB_VAL, sizeof(int32_t) * size_t(M)));
+    auto* key2 = static_cast<uint32_t*>(node_buffer(p, P::NB_KEY2, sizeof(uint32_t) * size_t(M)));
+    auto* val2 = static_cast<int32_t*>(node_buffer(p, P::NB_VAL2, sizeof(int32_t) * size_t(M)));
+    auto* tcount = static_cast<int32_t*>(node_buffer(p, P::NB_TCOUNT, sizeof(int32_t) * size_t(nt + 1)));
+    void* scr = node_buffer(p, P::NB_SCR, sb);
+    if (!ti_u || !te_u || !key || !val || !key2 || !val2 || !tcount || !scr) {
+      free_nodes(p);
+      return NFFT_ERR_ALLOC;
+    }
+    NFFT_CUDA_TRY(cudaMemsetAsync(tcount, 0, sizeof(int32_t) * size_t(nt + 1), s));
+    rc = launch_reduce_nodes(p, p->k, ti_u, te_u, key, val, tcount);
     if (rc) return rc;
     uint32_t* ko = nullptr;
     int32_t* vo = nullptr;
-    rc = radix_sort_pairs(static_cast<uint32_t*>(key.p), static_cast<int32_t*>(val.p), static_cast<uint32_t*>(key2.p),
-                          static_cast<int32_t*>(val2.p), M, kbits, scr.p, sb, s, &ko, &vo);
+    rc = radix_sort_pairs(key, val, key2, val2, M, kbits, scr, sb, s, &ko, &vo);
     if (rc) return rc;
-    rc = exclusive_scan_i32(static_cast<int32_t*>(tcount.p), p->tile_start, nt + 1, scr.p, sb, s);
+    rc = exclusive_scan_i32(tcount, p->tile_start, nt + 1, scr, sb, s);
     if (rc) return rc;
-    rc = launch_build_node_tables(p, vo, static_cast<int32_t*>(ti_u.p), te_u.p);
+    rc = launch_build_node_tables(p, vo, ti_u, te_u);
     if (rc) return rc;
-    NFFT_CUDA_TRY(cudaStreamSynchronize(s));
   }
   if (table) {
     rc = launch_build_weight_table(p);
@@ -738,10 +761,8 @@ int nfft_set_nodes(nfft_plan* p, const void* k, int k_on_device) {
     }
     rc = launch_build_tasks(p, chunk);
     if (rc) return rc;
-    if (cudaMalloc(&p->fsorted, 2 * rs * size_t(M > 0 ? M : 1)) != cudaSuccess) {
-      set_error("cudaMalloc of the sorted value buffer failed");
-      return NFFT_ERR_ALLOC;
-    }
+    p->fsorted = node_buffer(p, P::NB_FSORTED, 2 * rs * size_t(M));
+    if (!p->fsorted) return NFFT_ERR_ALLOC;
     p->scratch_bytes += sizeof(int4) * size_t(p->n_tasks) + 2 * rs * size_t(M);
   }
   NFFT_CUDA_TRY(cudaStreamSynchronize(s));

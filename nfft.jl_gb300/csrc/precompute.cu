@@ -5,6 +5,8 @@
 
 #include <math.h>
 
+#include <algorithm>
+
 namespace nfft {
 namespace {
 
@@ -240,48 +242,27 @@ int launch_deconv_factors(nfft_plan* p) {
 // at most `chunk` nodes.  Allocates p->tasks.
 int launch_build_tasks(nfft_plan* p, int chunk) {
   const int64_t nt = p->ntiles_total;
-  int32_t *tcnt = nullptr, *toff = nullptr;
-  void* scr = nullptr;
-  int rc = NFFT_OK;
   const size_t sb = scan_scratch_bytes(nt + 1);
-  if (cudaMalloc(&tcnt, sizeof(int32_t) * (nt + 1)) != cudaSuccess ||
-      cudaMalloc(&toff, sizeof(int32_t) * (nt + 1)) != cudaSuccess || cudaMalloc(&scr, sb) != cudaSuccess) {
-    set_error("cudaMalloc failed while building spreading tasks");
-    rc = NFFT_ERR_ALLOC;
-  }
+  auto* tcnt = static_cast<int32_t*>(node_buffer(p, nfft_plan::NB_TCNT, sizeof(int32_t) * (nt + 1)));
+  auto* toff = static_cast<int32_t*>(node_buffer(p, nfft_plan::NB_TOFF, sizeof(int32_t) * (nt + 1)));
+  void* scr = node_buffer(p, nfft_plan::NB_SCR, std::max(sb, p->nbuf_cap[nfft_plan::NB_SCR]));
+  if (!tcnt || !toff || !scr) return NFFT_ERR_ALLOC;
+  task_counts_kernel<<<unsigned((nt + 255) / 256), 256, 0, p->stream>>>(p->tile_start, nt, chunk, tcnt);
+  NFFT_LAUNCH_CHECK();
+  NFFT_CUDA_TRY(cudaMemsetAsync(tcnt + nt, 0, sizeof(int32_t), p->stream));
+  int rc = exclusive_scan_i32(tcnt, toff, nt + 1, scr, p->nbuf_cap[nfft_plan::NB_SCR], p->stream);
+  if (rc) return rc;
   int32_t ntasks = 0;
-  if (!rc) {
-    task_counts_kernel<<<unsigned((nt + 255) / 256), 256, 0, p->stream>>>(p->tile_start, nt, chunk, tcnt);
-    g_launches.fetch_add(1);
-    cudaMemsetAsync(tcnt + nt, 0, sizeof(int32_t), p->stream);
-    rc = exclusive_scan_i32(tcnt, toff, nt + 1, scr, sb, p->stream);
-  }
-  if (!rc) {
-    cudaMemcpyAsync(&ntasks, toff + nt, sizeof(int32_t), cudaMemcpyDeviceToHost, p->stream);
-    if (cudaStreamSynchronize(p->stream) != cudaSuccess) {
-      set_error("stream sync failed while building spreading tasks");
-      rc = NFFT_ERR_CUDA;
-    }
-  }
-  if (!rc) {
-    p->n_tasks = ntasks;
-    if (cudaMalloc(&p->tasks, sizeof(int4) * size_t(ntasks > 0 ? ntasks : 1)) != cudaSuccess) {
-      set_error("cudaMalloc failed for spreading tasks");
-      rc = NFFT_ERR_ALLOC;
-    }
-  }
-  if (!rc && ntasks > 0) {
+  NFFT_CUDA_TRY(cudaMemcpyAsync(&ntasks, toff + nt, sizeof(int32_t), cudaMemcpyDeviceToHost, p->stream));
+  NFFT_CUDA_TRY(cudaStreamSynchronize(p->stream));  // the task count sizes the launches
+  p->n_tasks = ntasks;
+  p->tasks = static_cast<int4*>(node_buffer(p, nfft_plan::NB_TASKS, sizeof(int4) * size_t(ntasks)));
+  if (!p->tasks) return NFFT_ERR_ALLOC;
+  if (ntasks > 0) {
     fill_tasks_kernel<<<unsigned((nt + 255) / 256), 256, 0, p->stream>>>(p->tile_start, toff, nt, chunk, p->tasks);
-    g_launches.fetch_add(1);
-    if (cudaStreamSynchronize(p->stream) != cudaSuccess || cudaGetLastError() != cudaSuccess) {
-      set_error("building spreading tasks failed");
-      rc = NFFT_ERR_CUDA;
-    }
+    NFFT_LAUNCH_CHECK();
   }
-  cudaFree(tcnt);
-  cudaFree(toff);
-  cudaFree(scr);
-  return rc;
+  return NFFT_OK;
 }
 
 }  // namespace nfft
