@@ -380,13 +380,13 @@ __global__ void __launch_bounds__(kInterpThreads) interp_tile3_kernel(const __gr
 }
 
 template <int BX, int BY, int BZ>
-int interp_tile3_launch(const nfft_plan* p, const Geom<float>& G, const Nodes<float>& Nd, const float2* g,
-                        float2* fhat) {
+int interp_tile3_launch(const nfft_plan* p, const CUtensorMap* map, const Geom<float>& G, const Nodes<float>& Nd,
+                        const float2* g, float2* fhat) {
   using TC = Tile3<BX, BY, BZ>;
   const size_t smem = TC::ACC_BYTES + 16;
   auto kern = p->wtab ? interp_tile3_kernel<BX, BY, BZ, true> : interp_tile3_kernel<BX, BY, BZ, false>;
   NFFT_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
-  kern<<<unsigned(p->n_tasks), kInterpThreads, smem, p->stream>>>(p->tmap, G, Nd, p->tasks, g, fhat, p->dflag + 1);
+  kern<<<unsigned(p->n_tasks), kInterpThreads, smem, p->stream>>>(*map, G, Nd, p->tasks, g, fhat, p->dflag + 1);
   NFFT_LAUNCH_CHECK();
   return NFFT_OK;
 }
@@ -398,11 +398,12 @@ int interp_tile3(const nfft_plan* cp, const Geom<float>& G, const Nodes<float>& 
   if (!p->gather_tma || !p->tasks || p->n_tasks == 0 || !tile3_shape(p)) return -1;
   void* gv = const_cast<float2*>(g);
   const int64_t bx = p->bs[0], by = p->bs[1];
-  if (bx == 16 && by == 8) return tile3_map<16, 8, 8>(p, gv) ? interp_tile3_launch<16, 8, 8>(p, G, Nd, g, fhat) : -1;
+  const CUtensorMap* map = nullptr;
+  if (bx == 16 && by == 8) return (map = tile3_map<16, 8, 8>(p, gv)) ? interp_tile3_launch<16, 8, 8>(p, map, G, Nd, g, fhat) : -1;
   if (bx == 16 && by == 16)
-    return tile3_map<16, 16, 8>(p, gv) ? interp_tile3_launch<16, 16, 8>(p, G, Nd, g, fhat) : -1;
-  if (bx == 32 && by == 8) return tile3_map<32, 8, 8>(p, gv) ? interp_tile3_launch<32, 8, 8>(p, G, Nd, g, fhat) : -1;
-  if (bx == 8 && by == 8) return tile3_map<8, 8, 8>(p, gv) ? interp_tile3_launch<8, 8, 8>(p, G, Nd, g, fhat) : -1;
+    return (map = tile3_map<16, 16, 8>(p, gv)) ? interp_tile3_launch<16, 16, 8>(p, map, G, Nd, g, fhat) : -1;
+  if (bx == 32 && by == 8) return (map = tile3_map<32, 8, 8>(p, gv)) ? interp_tile3_launch<32, 8, 8>(p, map, G, Nd, g, fhat) : -1;
+  if (bx == 8 && by == 8) return (map = tile3_map<8, 8, 8>(p, gv)) ? interp_tile3_launch<8, 8, 8>(p, map, G, Nd, g, fhat) : -1;
   return -1;
 }
 

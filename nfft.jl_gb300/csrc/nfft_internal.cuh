@@ -148,9 +148,20 @@ struct nfft_plan {
   bool spread_tile3 = true;        // 3-D FP32 m = 4: shape-specialised spreading kernel (spread_tile3.cuh)
   bool spread_tma = true;          // its bulk tensor reduction flush for tiles that do not wrap
   bool gather_tma = true;          // 3-D FP32 m = 4 gather from tiles loaded by bulk tensor copies
-  CUtensorMap tmap{};              // tensor map of the grid tmap_grid for that flush (shape tmap_key)
-  void* tmap_grid = nullptr;
-  int64_t tmap_key = 0;
+  // tensor maps of the grids the tiled kernels moved tiles of (the plan's two
+  // grids), with their grid and tile shape; replaced least recently made first
+  CUtensorMap tmap[2] = {};
+  void* tmap_grid[2] = {nullptr, nullptr};
+  int64_t tmap_key[2] = {0, 0};
+  int tmap_next = 0;
+  // a second grid for the adjoint, zeroed on a side stream beside the next
+  // forward transform's gather so that the next adjoint needs no memset
+  bool prezero = true;
+  bool grid2_dirty = false;        // grid2 holds an adjoint's data
+  void* grid2 = nullptr;
+  cudaStream_t zero_stream = nullptr;
+  cudaEvent_t ev_grid2_used = nullptr, ev_grid2_zeroed = nullptr;
+  bool skip_memset = false;        // set while the spreading target is known to be zero
   int gather_pitch = 0;            // shared-memory row pitch of the staged gather tile
   bool gather_tiled = false;       // gather from shared-memory tiles (else straight from L1/L2)
   // device buffers of nfft_set_nodes, kept across calls (nodes! every step of

@@ -2,6 +2,8 @@
 // node binning, forward/adjoint orchestration, cuFFT, timing, errors.
 #include "nfft_internal.cuh"
 
+#include <utility>
+
 #include <chrono>
 #include <cmath>
 #include <cstdarg>
@@ -558,6 +560,8 @@ int nfft_plan_create(nfft_plan** out, int precision, int D, const int64_t* N, in
   if (const char* e = getenv("NFFT_GB300_GATHER_TMA")) p->gather_tma = e[0] != '0';
   // the centred internal grid of the transforms (on by default)
   if (const char* e = getenv("NFFT_GB300_CENTER")) p->center = e[0] != '0';
+  // the adjoint's pre-zeroed second grid (on by default)
+  if (const char* e = getenv("NFFT_GB300_PREZERO")) p->prezero = e[0] != '0';
   p->ntiles_total = 1;
   for (int d = 0; d < 3; ++d) {
     p->ntiles[d] = (p->Nt[d] + p->bs[d] - 1) / p->bs[d];
@@ -648,6 +652,11 @@ int nfft_plan_create(nfft_plan** out, int precision, int D, const int64_t* N, in
 int nfft_plan_destroy(nfft_plan* p) {
   if (!p) return NFFT_OK;
   release_node_buffers(p);
+  if (p->zero_stream) cudaStreamSynchronize(p->zero_stream);
+  cudaFree(p->grid2);
+  if (p->zero_stream) cudaStreamDestroy(p->zero_stream);
+  if (p->ev_grid2_used) cudaEventDestroy(p->ev_grid2_used);
+  if (p->ev_grid2_zeroed) cudaEventDestroy(p->ev_grid2_zeroed);
   cudaFree(p->grid);
   cudaFree(p->inv);
   cudaFree(p->inv_c);
@@ -801,6 +810,8 @@ static int require_nodes(const nfft_plan* p) {
   return NFFT_OK;
 }
 
+static void zero_grid2_beside(nfft_plan* p);
+
 int nfft_forward(nfft_plan* p, const void* f, void* fhat) {
   int rc = require_nodes(p);
   if (rc) return rc;
@@ -813,6 +824,7 @@ int nfft_forward(nfft_plan* p, const void* f, void* fhat) {
   rc = p->fused_fft ? fused_forward_lines(p) : exec_fft(p, CUFFT_FORWARD);
   if (rc) return rc;
   record(p, slot, 2);
+  zero_grid2_beside(p);
   rc = p->prm.blocking ? launch_interp(p, p->grid, 0, fhat, 0) : launch_plain_interp(p, p->grid, 0, fhat, 0);
   if (rc) return rc;
   record(p, slot, 3);
@@ -820,10 +832,81 @@ int nfft_forward(nfft_plan* p, const void* f, void* fhat) {
   return NFFT_OK;
 }
 
+// The adjoint's second grid: allocated (and zeroed once, in stream order) on
+// first use.  After an adjoint it holds that adjoint's grid; the next forward
+// transform zeroes it on the plan's side stream beside its gather (which is
+// bound by on-chip traffic, so the memset's HBM writes cost it little), and
+// an adjoint that finds it not yet zeroed zeroes it in order.  Not used while
+// the plan's stream is being captured into a graph, for small grids (the
+// memset is cheap there) or when NFFT_GB300_PREZERO=0.
+static size_t grid_bytes(const nfft_plan* p) { return 2 * p->real_size * size_t(p->Nt[0] * p->Nt[1] * p->Nt[2]); }
+
+static bool capturing(const nfft_plan* p) {
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  return cudaStreamIsCapturing(p->stream, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone;
+}
+
+static void zero_grid2_beside(nfft_plan* p) {
+  if (!p->grid2_dirty || capturing(p)) return;
+  cudaEventRecord(p->ev_grid2_used, p->stream);
+  cudaStreamWaitEvent(p->zero_stream, p->ev_grid2_used, 0);
+  cudaMemsetAsync(p->grid2, 0, grid_bytes(p), p->zero_stream);
+  cudaEventRecord(p->ev_grid2_zeroed, p->zero_stream);
+  p->grid2_dirty = false;
+}
+
+static bool use_grid2(nfft_plan* p) {
+  const size_t bytes = grid_bytes(p);
+  if (!p->prezero || !p->prm.blocking || bytes < (size_t(64) << 20) || capturing(p)) return false;
+  if (!p->grid2) {
+    if (cudaMalloc(&p->grid2, bytes) != cudaSuccess) {
+      p->grid2 = nullptr;
+      p->prezero = false;  // not enough memory for the second grid: memset per adjoint
+      cudaGetLastError();
+      return false;
+    }
+    if (cudaStreamCreateWithFlags(&p->zero_stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&p->ev_grid2_used, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&p->ev_grid2_zeroed, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventRecord(p->ev_grid2_zeroed, p->stream) != cudaSuccess) {
+      p->prezero = false;
+      cudaGetLastError();
+      return false;
+    }
+    p->grid2_dirty = true;
+    p->scratch_bytes += bytes;
+  }
+  if (p->grid2_dirty) {  // no forward transform since the last adjoint
+    if (cudaMemsetAsync(p->grid2, 0, bytes, p->stream) != cudaSuccess) return false;
+    p->grid2_dirty = false;
+  }
+  return true;
+}
+
+// Swaps the plan's grid with the zeroed second grid for one adjoint; on exit
+// swaps back and marks the second grid as holding data.
+struct Grid2Scope {
+  nfft_plan* p;
+  bool on;
+  explicit Grid2Scope(nfft_plan* q) : p(q), on(use_grid2(q)) {
+    if (!on) return;
+    cudaStreamWaitEvent(p->stream, p->ev_grid2_zeroed, 0);
+    std::swap(p->grid, p->grid2);
+    p->skip_memset = true;
+  }
+  ~Grid2Scope() {
+    if (!on) return;
+    std::swap(p->grid, p->grid2);
+    p->skip_memset = false;
+    p->grid2_dirty = true;
+  }
+};
+
 int nfft_adjoint(nfft_plan* p, const void* fhat, void* f) {
   int rc = require_nodes(p);
   if (rc) return rc;
   CenterScope centred(p);
+  Grid2Scope zeroed(p);
   const int slot = p->timing_on ? ring_slot(p) : 0;
   record(p, slot, 0);
   rc = p->prm.blocking ? launch_spread(p, fhat, 0, p->grid, 0) : launch_plain_spread(p, fhat, 0, p->grid, 0);

@@ -59,12 +59,13 @@ template <int BX, int BY, int BZ>
 int tile3_launch(nfft_plan* p, const Geom<float>& G, const Nodes<float>& Nd, const float2* fs, float* gp, int ncols,
                  int64_t fcol, int64_t gcol_t) {
   using TC = Tile3<BX, BY, BZ>;
-  const int use_tma = (ncols == 1 && p->spread_tma && tile3_map<BX, BY, BZ>(p, gp)) ? 1 : 0;
+  const CUtensorMap* map = (ncols == 1 && p->spread_tma) ? tile3_map<BX, BY, BZ>(p, gp) : nullptr;
+  const int use_tma = map ? 1 : 0;
   auto kern = p->wtab ? spread_tile3_kernel<BX, BY, BZ, true> : spread_tile3_kernel<BX, BY, BZ, false>;
   NFFT_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(TC::SMEM)));
   CUtensorMap none{};
   kern<<<dim3(unsigned(p->n_tasks), unsigned(ncols)), TC::THREADS, TC::SMEM, p->stream>>>(
-      use_tma ? p->tmap : none, use_tma, G, Nd, p->tasks, fs, gp, ncols > 1 ? fcol : 0, gcol_t);
+      map ? *map : none, use_tma, G, Nd, p->tasks, fs, gp, ncols > 1 ? fcol : 0, gcol_t);
   NFFT_LAUNCH_CHECK();
   return NFFT_OK;
 }
@@ -92,7 +93,7 @@ int spread_launch(nfft_plan* p, const void* fhat, void* g, int ncols, int64_t fc
   Nodes<T> Nd = make_nodes<T>(p);
   using C = typename Cplx<T>::type;
   const size_t gbytes = size_t(p->Nt[0] * p->Nt[1] * p->Nt[2]) * sizeof(T) * 2;
-  NFFT_CUDA_TRY(cudaMemsetAsync(g, 0, gbytes * size_t(ncols), p->stream));
+  if (!p->skip_memset) NFFT_CUDA_TRY(cudaMemsetAsync(g, 0, gbytes * size_t(ncols), p->stream));
   if (p->n_tasks == 0) return NFFT_OK;
   const C* fp = static_cast<const C*>(fhat);
   T* gp = static_cast<T*>(g);

@@ -74,27 +74,31 @@ EncodeTiledFn encode_tiled() {
 
 // Tensor map of the FP32 grid g (2 Ntilde[0] floats x Ntilde[1] x Ntilde[2])
 // with the padded-tile box of Tile3<BX, BY, BZ>, cached on the plan per grid
-// and shape.  False when it cannot be made (no driver entry point, grid not
-// 16-byte aligned, box larger than the grid): the kernel then flushes per point.
-template <int BX, int BY, int BZ> bool tile3_map(nfft_plan* p, void* g) {
+// and shape (two entries: the plan's forward and adjoint grids).  Null when it
+// cannot be made (no driver entry point, grid not 16-byte aligned, box larger
+// than the grid): the kernels then move tiles point by point.
+template <int BX, int BY, int BZ> const CUtensorMap* tile3_map(nfft_plan* p, void* g) {
   using TC = Tile3<BX, BY, BZ>;
   const int64_t key = (int64_t(BX) << 20) | (int64_t(BY) << 10) | BZ;
-  if (p->tmap_grid == g && p->tmap_key == key) return true;
-  p->tmap_grid = nullptr;
+  for (int i = 0; i < 2; ++i)
+    if (p->tmap_grid[i] == g && p->tmap_key[i] == key) return &p->tmap[i];
   EncodeTiledFn fn = encode_tiled();
-  if (!fn || (reinterpret_cast<uintptr_t>(g) & 15) != 0) return false;
-  if (p->Nt[0] < TC::PITCH || p->Nt[1] < TC::P1 || p->Nt[2] < TC::P2) return false;
+  if (!fn || (reinterpret_cast<uintptr_t>(g) & 15) != 0) return nullptr;
+  if (p->Nt[0] < TC::PITCH || p->Nt[1] < TC::P1 || p->Nt[2] < TC::P2) return nullptr;
+  const int slot = p->tmap_next;
+  p->tmap_grid[slot] = nullptr;
   const cuuint64_t dims[3] = {cuuint64_t(2 * p->Nt[0]), cuuint64_t(p->Nt[1]), cuuint64_t(p->Nt[2])};
   const cuuint64_t strides[2] = {cuuint64_t(8 * p->Nt[0]), cuuint64_t(8 * p->Nt[0] * p->Nt[1])};
   const cuuint32_t box[3] = {cuuint32_t(2 * TC::PITCH), cuuint32_t(TC::P1), cuuint32_t(TC::P2)};
   const cuuint32_t es[3] = {1, 1, 1};
-  if (fn(&p->tmap, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, g, dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
+  if (fn(&p->tmap[slot], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, g, dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
          CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) !=
       CUDA_SUCCESS)
-    return false;
-  p->tmap_grid = g;
-  p->tmap_key = key;
-  return true;
+    return nullptr;
+  p->tmap_grid[slot] = g;
+  p->tmap_key[slot] = key;
+  p->tmap_next = slot ^ 1;
+  return &p->tmap[slot];
 }
 
 }  // namespace

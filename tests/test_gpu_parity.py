@@ -367,3 +367,34 @@ def test_specialised_3d_gather(monkeypatch, bs, pre, tma):
     p.convolve_(nf.as_colmajor(grid, p.Ñ, p.cdtype), out)
     assert oracle.rel_l2(out.cpu().numpy(), op.convolve(grid)) < TOL32
     assert nf.load().nfft_sync(p._handle) == 0
+
+
+def test_adjoint_second_grid(monkeypatch):
+    """Adjoints of a plan whose grid is at least 64 MB spread into a second
+    grid zeroed on a side stream after the previous adjoint: adjoints
+    interleaved with forward transforms give the oracle's adjoint every time,
+    and the same values as a plan that zeroes its one grid per adjoint."""
+    N = (128, 128, 128)
+    k, f, fhat = rand_problem(3, N, 50000, seed=302, dtype=np.float32)
+    rng = np.random.default_rng(7)
+    fhat2 = (rng.standard_normal(k.shape[1]) + 1j * rng.standard_normal(k.shape[1])).astype(np.complex64)
+    op = oracle.OraclePlan(k.astype(np.float64), N, m=4, sigma=2.0)
+    refs = [colmajor_flat(op.adjoint(fhat)), colmajor_flat(op.adjoint(fhat2))]
+    yref = op.forward(f)
+    outs = {}
+    for prezero in ("1", "0"):
+        monkeypatch.setenv("NFFT_GB300_PREZERO", prezero)
+        p = nf.plan_nfft(k, N, m=4, sigma=2.0)
+        a = nf.adjoint(p)
+        xs = []
+        for i, v in enumerate([fhat, fhat2, fhat, fhat2]):
+            xs.append(colmajor_flat((a * torch.as_tensor(v).to(p.cdtype)).cpu().numpy()))
+            if i == 1:
+                y = (p * nf.as_colmajor(f, N, p.cdtype)).cpu().numpy()
+                assert oracle.rel_l2(y, yref) < TOL32
+        for i, x in enumerate(xs):
+            assert oracle.rel_l2(x, refs[i % 2]) < TOL32
+        assert nf.load().nfft_sync(p._handle) == 0
+        outs[prezero] = xs
+    for x1, x0 in zip(outs["1"], outs["0"]):
+        assert oracle.rel_l2(x1, x0) < 1e-6
