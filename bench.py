@@ -965,6 +965,9 @@ def run_extras(args):
       a directional plan: 2-D NFFTs (dims 1:2) of the 64 slices of a
       256 x 256 x 64 stack, 2-D radial nodes (256 spokes x 512 samples),
       against 64 single 2-D plans;
+      a directional plan whose transform dims follow a column index (dims 2:3
+      of a 64 x 256 x 256 stack, same nodes), tiled path against the atomic
+      per-(column, node) path;
       3-D NFCT and NFST plans, N = 64^3, 2^20 nodes in [0, 1/2)^3 (fwd +
       transpose, error vs the direct GPU sums on 64 nodes);
       NFFTTools' sdc (20 iterations) on the 2-D spiral (config 5's nodes)."""
@@ -1058,6 +1061,27 @@ def run_extras(args):
          dtype="f32", loop_of_64_single_2d_plans={"ms_per_step": t_loop * 1e3, "speedup_of_value": t_loop / t_dir},
          rel_diff_slice5_vs_single_plan=d5)
     del pd, ps, fd, vd, yd, xd, fsl, vsl
+    torch.cuda.empty_cache()
+
+    # ---- directional, transform dims after a column index: dims 2:3 of a 64 x 256 x 256 stack
+    Nq = (64, 256, 256)
+    fq = nf.as_colmajor(complex_normal(rng, Nq), Nq, torch.complex64, dev)
+    t_q = {}
+    for tiled in ("1", "0"):
+        os.environ["NFFT_GB300_DIRECTIONAL_TILED"] = tiled
+        pq = nf.plan_nfft(k2, Nq, dims=(2, 3), m=4, sigma=2.0)
+        vq = nf.as_colmajor(complex_normal(rng, pq.NOut), pq.NOut, torch.complex64, dev)
+        yq = nf.empty_image(pq.NOut, torch.complex64, dev)
+        xq = nf.empty_image(Nq, torch.complex64, dev)
+        t_q[tiled] = timed(lambda: (pq.forward_(yq, fq), pq.adjoint_(xq, vq)))
+        del pq, vq, yq, xq
+    os.environ.pop("NFFT_GB300_DIRECTIONAL_TILED", None)
+    emit("directional 2-D NFFT (dims 2:3) of a 64x256x256 stack: fwd+adj node values/s", J * Nq[0] / t_q["1"],
+         "node values/s", t_q["1"] * 1e3,
+         {"workload": "N=(64,256,256), dims=2:3 (64 columns before the transform dims), the 2-D radial nodes "
+                      "above (J=131072), KB m=4 sigma=2, LINEAR"},
+         dtype="f32", atomic_path={"ms_per_step": t_q["0"] * 1e3, "speedup_of_value": t_q["0"] / t_q["1"]})
+    del fq
     torch.cuda.empty_cache()
 
     # ---- 3-D NFCT / NFST

@@ -5,13 +5,22 @@
 // forces precompute = LINEAR and runs unblocked loops.
 //
 // GB300 form: the data is (pre, transform dims, post) with pre the
-// contiguous inner index.  One kernel per stage covers all columns:
-//   pad + apodize  g[pre, (n + Ntilde - N/2) mod Ntilde, post] = f * prod 1/phi-hat
-//   FFT            cuFFT along dims, batched over the columns
-//   gather         thread per (pre, node, post), pre fastest (coalesced columns)
-//   spread         same mapping, global atomics (the reference's unblocked
-//                  convolve_transpose! of src/directional.jl:107-154)
-//   crop + apodize
+// contiguous inner index.  Every (pre, post) index pair is a column: an image
+// of the transform dims.  The core plan bins the nodes once, and the columns
+// are transformed together:
+//   pad + apodize  grid column c = a + pre b holds image column (a, b) at
+//                  (n + Ntilde - N/2) mod Ntilde, times prod 1/phi-hat; for
+//                  pre > 1 a shared-memory transposition (pre <-> image index)
+//   FFT            cuFFT along dims, batched over the contiguous grid columns
+//   gather         the core plan's tiled gather, all columns per launch, into
+//                  node values in column order, transposed to (pre, node, post)
+//   spread         node values transposed to column order, then the core
+//                  plan's atomic-free tiled spreader, all columns per launch
+//   crop + apodize (transposing for pre > 1)
+// Plans without nodes (and pre > 1 with NFFT_GB300_DIRECTIONAL_TILED=0) keep
+// the grid in (pre, grid, post) order and run one thread per (pre, node, post)
+// with global atomics for the spread (the reference's unblocked
+// convolve_transpose! of src/directional.jl:107-154).
 // The window follows src/directional.jl:82-92: xscale = k * Ntilde in T,
 // c = floor(xscale), taps c-m+1 .. c+m, LUT linear interpolation at
 // |xscale - l| * LUTSize/m.  A core plan over the transform dims supplies the
@@ -39,11 +48,12 @@ struct nfft_dplan {
   bool fft_loop = false;           // one exec per post column block
   void* fft_work = nullptr;
   bool has_nodes = false;
-  // pre == 1 (the transform dims lead): every column is an ordinary image of
-  // the transform dims, so the core plan bins the nodes once and its tiled
-  // gather / atomic-free spreader run column by column
+  // tiled: grid columns contiguous (column c = a + pre b), the core plan's
+  // tiled gather / atomic-free spreader run over all columns
   bool tiled = false;
-  void* sorted = nullptr;          // tiled: bin-sorted node values of every column (M x post complex)
+  int64_t ncols = 1;               // pre x post
+  void* sorted = nullptr;          // tiled: bin-sorted node values of a launch's columns (M x <= 65535 complex)
+  void* vals = nullptr;            // tiled, pre > 1: node values in column order (M x ncols complex)
 };
 
 namespace nfft {
@@ -149,6 +159,98 @@ __global__ void __launch_bounds__(256) dcrop_kernel(DGeom<T> G, const typename C
     v.y = s.y * w;
     f[q] = v;
   }
+}
+
+// Grid offset within a column (uncentred oversampled grid) and apodization
+// factor of image point n of the transform dims.
+template <typename T> __device__ __forceinline__ int64_t dgrid_point(const DGeom<T>& G, int64_t n, T& w) {
+  int64_t gl = 0, stride = 1;
+  w = T(1);
+  for (int d = 0; d < G.R; ++d) {
+    const int nd = int(n % G.N[d]);
+    n /= G.N[d];
+    gl += int64_t(wrap_once(nd - G.N[d] / 2, G.Nt[d])) * stride;
+    w *= __ldg(G.inv[d] + nd);
+    stride *= G.Nt[d];
+  }
+  return gl;
+}
+
+// Transposition between the user layout X[a + pre (n + nn b)] (pre index a
+// contiguous) and the column layout Y[map(n) + ystride (a + pre b)] through a
+// 32 x 32 shared-memory tile, both sides coalesced.  GRID: n is an image
+// point, map(n) its grid offset, values scaled by its apodization factor
+// (pad: X -> Y into a zeroed grid; crop: Y -> X); otherwise map(n) = n
+// (node values).  Block 32 x 8; grid (n tiles, a tiles, post).
+template <typename T, bool TO_Y, bool GRID>
+__global__ void __launch_bounds__(256) dtranspose_kernel(DGeom<T> G, const typename Cplx<T>::type* __restrict__ src,
+                                                         typename Cplx<T>::type* __restrict__ dst, int64_t nn,
+                                                         int64_t ystride) {
+  using C = typename Cplx<T>::type;
+  __shared__ C tile[32][33];
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+  const int64_t n0 = int64_t(blockIdx.x) * 32, a0 = int64_t(blockIdx.y) * 32;
+  // the n of this thread on the column side, with its grid offset and factor
+  const int64_t nc = n0 + tx;
+  T w = T(1);
+  int64_t yoff = nc;
+  if (GRID && nc < nn) yoff = dgrid_point(G, nc, w);
+  for (int64_t b = blockIdx.z; b < G.post; b += gridDim.z) {
+    const int64_t xbase = G.pre * nn * b, cbase = G.pre * b;
+    if (TO_Y) {
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {  // X rows n, coalesced over a
+        const int64_t n = n0 + ty + 8 * i, a = a0 + tx;
+        if (n < nn && a < G.pre) tile[ty + 8 * i][tx] = src[xbase + a + G.pre * n];
+      }
+      __syncthreads();
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {  // Y columns a, coalesced over n
+        const int64_t a = a0 + ty + 8 * i;
+        if (nc < nn && a < G.pre) {
+          C v = tile[tx][ty + 8 * i];
+          v.x *= w;
+          v.y *= w;
+          dst[yoff + ystride * (cbase + a)] = v;
+        }
+      }
+    } else {
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {  // Y columns a, coalesced over n
+        const int64_t a = a0 + ty + 8 * i;
+        if (nc < nn && a < G.pre) {
+          C v = src[yoff + ystride * (cbase + a)];
+          v.x *= w;
+          v.y *= w;
+          tile[tx][ty + 8 * i] = v;
+        }
+      }
+      __syncthreads();
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {  // X rows n, coalesced over a
+        const int64_t n = n0 + ty + 8 * i, a = a0 + tx;
+        if (n < nn && a < G.pre) dst[xbase + a + G.pre * n] = tile[ty + 8 * i][tx];
+      }
+    }
+    __syncthreads();
+  }
+}
+
+template <typename T, bool TO_Y, bool GRID>
+int dtranspose(nfft_dplan* q, const DGeom<T>& G, const void* src, void* dst, int64_t nn, int64_t ystride) {
+  using C = typename Cplx<T>::type;
+  if (nn == 0) return NFFT_OK;
+  const int64_t nt = (nn + 31) / 32, at = (q->pre + 31) / 32;
+  if (at > 65535) {
+    set_error("directional plan: %lld columns before dims exceed the transposition grid", (long long)q->pre);
+    return NFFT_ERR_UNSUPPORTED;
+  }
+  if (nt > 0x7fffffffLL) return NFFT_ERR_UNSUPPORTED;
+  const unsigned gz = unsigned(q->post < 65535 ? q->post : 65535);
+  dtranspose_kernel<T, TO_Y, GRID><<<dim3(unsigned(nt), unsigned(at), gz), 256, 0, q->stream>>>(
+      G, static_cast<const C*>(src), static_cast<C*>(dst), nn, ystride);
+  NFFT_LAUNCH_CHECK();
+  return NFFT_OK;
 }
 
 // Window values and first grid index of node j along transform dim d.
@@ -300,42 +402,67 @@ int dexec_fft(nfft_dplan* q, int dir) {
   return NFFT_OK;
 }
 
+// All columns' gather (tiled) from the contiguous grid columns into
+// node values out[j + M c], at most 65535 columns per launch.
+template <typename T> int dgather_cols(nfft_dplan* q, void* out) {
+  using C = typename Cplx<T>::type;
+  int rc = NFFT_OK;
+  for (int64_t c0 = 0; c0 < q->ncols && !rc; c0 += 65535) {
+    const int nc = int(q->ncols - c0 < 65535 ? q->ncols - c0 : 65535);
+    rc = launch_interp_cols(q->core, static_cast<const C*>(q->grid) + c0 * q->Rnt, static_cast<C*>(out) + c0 * q->M,
+                            nc, q->Rnt, q->M);
+  }
+  return rc;
+}
+
+// All columns' spread (tiled, atomic-free) of node values in[j + M c] into
+// the contiguous grid columns (the spreader zeroes them).
+template <typename T> int dspread_cols(nfft_dplan* q, const void* in) {
+  using C = typename Cplx<T>::type;
+  int rc = NFFT_OK;
+  for (int64_t c0 = 0; c0 < q->ncols && !rc; c0 += 65535) {
+    const int nc = int(q->ncols - c0 < 65535 ? q->ncols - c0 : 65535);
+    rc = launch_spread_cols(q->core, static_cast<const C*>(in) + c0 * q->M, static_cast<C*>(q->grid) + c0 * q->Rnt, nc,
+                            q->M, q->Rnt, q->sorted);
+  }
+  return rc;
+}
+
 template <typename T> int dforward(nfft_dplan* q, const void* f, void* fhat) {
   using C = typename Cplx<T>::type;
   DGeom<T> G = make_dgeom<T>(q);
-  dpad_kernel<T><<<blocks_for(q->pre * q->Rnt * q->post), 256, 0, q->stream>>>(G, static_cast<const C*>(f),
-                                                                               static_cast<C*>(q->grid));
-  NFFT_LAUNCH_CHECK();
-  int rc = dexec_fft(q, CUFFT_FORWARD);
-  if (rc) return rc;
-  if (q->tiled) {  // all columns in one launch (at most 65535 per launch)
-    for (int64_t c0 = 0; c0 < q->post && !rc; c0 += 65535) {
-      const int nc = int(q->post - c0 < 65535 ? q->post - c0 : 65535);
-      rc = launch_interp_cols(q->core, static_cast<const C*>(q->grid) + c0 * q->Rnt,
-                              static_cast<C*>(fhat) + c0 * q->M, nc, q->Rnt, q->M);
-    }
-    return rc;
+  int rc = NFFT_OK;
+  if (q->tiled && q->pre > 1) {  // transposing pad into zeroed grid columns
+    NFFT_CUDA_TRY(cudaMemsetAsync(q->grid, 0, 2 * sizeof(T) * size_t(q->ncols * q->Rnt), q->stream));
+    if ((rc = dtranspose<T, true, true>(q, G, f, q->grid, q->Rn, q->Rnt))) return rc;
+  } else {  // pre == 1: the layouts agree
+    dpad_kernel<T><<<blocks_for(q->pre * q->Rnt * q->post), 256, 0, q->stream>>>(G, static_cast<const C*>(f),
+                                                                                 static_cast<C*>(q->grid));
+    NFFT_LAUNCH_CHECK();
   }
-  return dconv<T>(q, q->grid, fhat, false);
+  if ((rc = dexec_fft(q, CUFFT_FORWARD))) return rc;
+  if (!q->tiled) return dconv<T>(q, q->grid, fhat, false);
+  if (q->pre == 1) return dgather_cols<T>(q, fhat);
+  if ((rc = dgather_cols<T>(q, q->vals))) return rc;
+  return dtranspose<T, false, false>(q, G, q->vals, fhat, q->M, q->M);
 }
 
 template <typename T> int dadjoint(nfft_dplan* q, const void* fhat, void* f) {
   using C = typename Cplx<T>::type;
   DGeom<T> G = make_dgeom<T>(q);
   int rc = NFFT_OK;
-  if (q->tiled) {  // the spreader zeroes the column grids itself
-    for (int64_t c0 = 0; c0 < q->post && !rc; c0 += 65535) {
-      const int nc = int(q->post - c0 < 65535 ? q->post - c0 : 65535);
-      rc = launch_spread_cols(q->core, static_cast<const C*>(fhat) + c0 * q->M, static_cast<C*>(q->grid) + c0 * q->Rnt,
-                              nc, q->M, q->Rnt, q->sorted);
-    }
+  if (q->tiled && q->pre > 1) {
+    if ((rc = dtranspose<T, true, false>(q, G, fhat, q->vals, q->M, q->M))) return rc;
+    rc = dspread_cols<T>(q, q->vals);
+  } else if (q->tiled) {
+    rc = dspread_cols<T>(q, fhat);
   } else {
     NFFT_CUDA_TRY(cudaMemsetAsync(q->grid, 0, 2 * sizeof(T) * size_t(q->pre * q->Rnt * q->post), q->stream));
     rc = dconv<T>(q, fhat, q->grid, true);
   }
   if (rc) return rc;
-  rc = dexec_fft(q, CUFFT_INVERSE);
-  if (rc) return rc;
+  if ((rc = dexec_fft(q, CUFFT_INVERSE))) return rc;
+  if (q->tiled && q->pre > 1) return dtranspose<T, false, true>(q, G, q->grid, f, q->Rn, q->Rnt);
   dcrop_kernel<T><<<blocks_for(q->pre * q->Rn * q->post), 256, 0, q->stream>>>(G, static_cast<const C*>(q->grid),
                                                                               static_cast<C*>(f));
   NFFT_LAUNCH_CHECK();
@@ -354,6 +481,7 @@ extern "C" int nfft_dplan_destroy(nfft_dplan* q) {
   cudaFree(q->grid);
   cudaFree(q->k);
   cudaFree(q->sorted);
+  cudaFree(q->vals);
   if (q->core) nfft_plan_destroy(q->core);
   delete q;
   return NFFT_OK;
@@ -390,7 +518,11 @@ extern "C" int nfft_dplan_create(nfft_dplan** out, int precision, int D, const i
   // the core plan: the transform dims, LINEAR window (src/implementation.jl:80-82)
   nfft_params prm = *params;
   prm.precompute = NFFT_PRECOMPUTE_LINEAR;
-  q->tiled = dim_lo == 0 && M > 0;
+  q->tiled = M > 0;
+  if (dim_lo > 0) {
+    const char* e = getenv("NFFT_GB300_DIRECTIONAL_TILED");
+    if (e && e[0] == '0') q->tiled = false;
+  }
   prm.blocking = q->tiled ? 1 : 0;
   prm.compensated = 0;
   prm.timing = 0;
@@ -415,11 +547,13 @@ extern "C" int nfft_dplan_create(nfft_dplan** out, int precision, int D, const i
     set_error("cudaMalloc of the directional grid failed");
     return NFFT_ERR_ALLOC;
   }
+  q->ncols = q->pre * q->post;
   if (q->tiled) {
-    const int64_t per = q->post < 65535 ? q->post : 65535;
-    if (cudaMalloc(&q->sorted, 2 * rs * size_t(M) * size_t(per)) != cudaSuccess) {
+    const int64_t per = q->ncols < 65535 ? q->ncols : 65535;
+    if (cudaMalloc(&q->sorted, 2 * rs * size_t(M) * size_t(per)) != cudaSuccess ||
+        (q->pre > 1 && cudaMalloc(&q->vals, 2 * rs * size_t(M) * size_t(q->ncols)) != cudaSuccess)) {
       nfft_dplan_destroy(q);
-      set_error("cudaMalloc of the sorted node values failed");
+      set_error("cudaMalloc of the column node values failed");
       return NFFT_ERR_ALLOC;
     }
   }
@@ -434,8 +568,9 @@ extern "C" int nfft_dplan_create(nfft_dplan** out, int precision, int D, const i
     r = cufftSetAutoAllocation(q->fft, 0);
   }
   if (r == CUFFT_SUCCESS) {
-    if (q->pre == 1) {
-      r = cufftMakePlanMany(q->fft, q->R, n, n, 1, int(q->Rnt), n, 1, int(q->Rnt), type, int(q->post), &ws);
+    if (q->pre == 1 || q->tiled) {  // contiguous grid columns
+      if (q->ncols > 0x7fffffffLL) r = CUFFT_INVALID_SIZE;
+      else r = cufftMakePlanMany(q->fft, q->R, n, n, 1, int(q->Rnt), n, 1, int(q->Rnt), type, int(q->ncols), &ws);
     } else {
       q->fft_loop = q->post > 1;
       r = cufftMakePlanMany(q->fft, q->R, n, n, int(q->pre), 1, n, int(q->pre), 1, type, int(q->pre), &ws);
