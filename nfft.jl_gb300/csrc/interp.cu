@@ -256,7 +256,9 @@ __global__ void __launch_bounds__(kInterpThreads) interp_tile_kernel(Geom<T> G, 
 // mbarrier), and each warp then interpolates one node at a time from shared
 // memory: lane (x = lane mod 8, row = lane / 8) reads its 8 z values of rows
 // iy and iy + 4 at constant offsets (16 loads, 2 wavefronts each), sums over
-// z, weights by phi_x phi_y and the warp adds the 32 partial sums.  Tiles
+// z and weights by phi_x phi_y; the warp adds the 32 partial sums of four
+// nodes at once.  Window values come straight from the table (broadcast
+// loads): shuffles share the shared-memory pipe with the tile reads.  Tiles
 // whose box wraps around the grid gather their nodes straight from L1/L2 as
 // interp_kernel does.  The wait for the copy is bounded: on timeout the CTA
 // raises status word 1 (reported by nfft_sync) and skips its nodes.
@@ -276,6 +278,16 @@ __device__ __forceinline__ bool mbar_try_wait(unsigned addr, unsigned parity) {
       : "memory");
   return ok != 0;
 }
+
+// Per-warp staging of the TMA gather: NK nodes per group, WCH 16-byte chunks
+// of window data per node (24 table values, or the 4 fractional offsets),
+// one slot = NK records + NK window blocks; two slots per warp.
+template <bool TABLE> struct Tile3Gather {
+  static constexpr int NK = 4;
+  static constexpr int WCH = TABLE ? 6 : 1;
+  static constexpr int SLOT = NK * (16 + 16 * WCH);
+  static constexpr size_t STAGE_BYTES = size_t(kInterpThreads / 32) * 2 * SLOT;
+};
 
 template <int BX, int BY, int BZ, bool TABLE>
 __global__ void __launch_bounds__(kInterpThreads) interp_tile3_kernel(const __grid_constant__ CUtensorMap tmap,
@@ -310,15 +322,32 @@ __global__ void __launch_bounds__(kInterpThreads) interp_tile3_kernel(const __gr
     for (int64_t i = task.y + warp; i < task.z; i += NWARPS) interp_node<3, 8, float, TABLE>(G, Nd, P, i, lane, g, fhat);
     return;
   }
-  // the first node's record and window values are loaded while the tile arrives
+  // Warp w takes the nodes task.y + NK w + NK NWARPS j + k, k < NK: the NK
+  // nodes' partial sums are reduced together (transposed butterfly: 3
+  // shuffles per node and component instead of 5).  The node records and
+  // window data (table values, or fractional offsets for Horner) of the next
+  // group are copied into the warp's other stage slot by cp.async while this
+  // group is summed; the first group's while the tile arrives.
+  constexpr int NK = Tile3Gather<TABLE>::NK, WCH = Tile3Gather<TABLE>::WCH, SLOT = Tile3Gather<TABLE>::SLOT;
   const int ix = lane & 7, ry = lane >> 3;
-  int64_t i = task.y + warp;
-  int4 nd = make_int4(0, 0, 0, 0);
-  float W[LN::NW];
-  if (i < task.z) {
-    nd = __ldg(Nd.node4 + i);
-    node_weights<3, 8, float, TABLE>(Nd, P, i, lane, W);
-  }
+  unsigned char* stage_base = smem_raw + TC::ACC_BYTES + 16 + warp * 2 * SLOT;
+  auto stage = [&](int buf, int64_t gbase) {
+    unsigned char* st = stage_base + buf * SLOT;
+    if (lane < NK * WCH) {
+      const int k = lane / WCH, c = lane % WCH;
+      const int64_t id = gbase + k;
+      if (id < task.z) {
+        const float* src = TABLE ? Nd.wtab + id * 24 + 4 * c : Nd.frac4 + 4 * id;
+        cp_async_elem(reinterpret_cast<float4*>(st + NK * 16 + k * 16 * WCH + 16 * c),
+                      reinterpret_cast<const float4*>(src));
+      }
+    } else if (lane >= 24 && lane < 24 + NK) {
+      const int64_t id = gbase + (lane - 24);
+      if (id < task.z) cp_async_elem(reinterpret_cast<int4*>(st) + (lane - 24), Nd.node4 + id);
+    }
+    asm volatile("cp.async.commit_group;" ::: "memory");
+  };
+  stage(0, task.y + NK * warp);
   if (threadIdx.x == 0) {
     mbar_init(mbar_s, 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -335,55 +364,92 @@ __global__ void __launch_bounds__(kInterpThreads) interp_tile3_kernel(const __gr
   bool done = false;
   for (int it = 0; it < (1 << 22) && !done; ++it) done = mbar_try_wait(mbar_s, 0);
   if (!done) {
+    asm volatile("cp.async.wait_all;" ::: "memory");  // no copy into shared memory outlives the CTA
     if (threadIdx.x == 0) atomicOr(status, 1);
     return;
   }
-  for (; i < task.z; i += NWARPS) {
-    // software pipeline: the next node's global loads are issued before this node's sums
-    const int64_t in = i + NWARPS;
-    int4 ndn = nd;
-    float Wn[LN::NW];
-    if (in < task.z) {
-      ndn = __ldg(Nd.node4 + in);
-      node_weights<3, 8, float, TABLE>(Nd, P, in, lane, Wn);
-    }
-    const float wx = wsel<3, 8>(W, ix);
-    const float wy0 = wsel<3, 8>(W, 8 + ry), wy1 = wsel<3, 8>(W, 12 + ry);
-    const float2* base = tile + (nd.z - o2) * PLANE + (nd.y - o1 + ry) * PITCH + (nd.x - o0 + 1) + ix;
-    float2 v0[8], v1[8];
+  int buf = 0;
+  for (int64_t base = task.y + NK * warp; base < task.z; base += NK * NWARPS) {
+    stage(buf ^ 1, base + NK * NWARPS);
+    asm volatile("cp.async.wait_group 1;" ::: "memory");  // this group's slot has landed
+    __syncwarp();
+    const unsigned char* st = stage_base + buf * SLOT;
+    const int4* rec = reinterpret_cast<const int4*>(st);
+    const float* win = reinterpret_cast<const float*>(st + NK * 16);
+    float ar[NK], ai[NK];
 #pragma unroll
-    for (int iz = 0; iz < 8; ++iz) {
-      v0[iz] = base[iz * PLANE];
-      v1[iz] = base[iz * PLANE + 4 * PITCH];
-    }
-    float s0r = 0.f, s0i = 0.f, s1r = 0.f, s1i = 0.f;
+    for (int k = 0; k < NK; ++k) {
+      ar[k] = 0.f;
+      ai[k] = 0.f;
+      if (base + k >= task.z) continue;  // warp-uniform
+      const int4 nd = rec[k];
+      // window values: x at the lane's column, y at its two rows, all 8 z
+      float wx, wy0, wy1, wz[8];
+      if constexpr (TABLE) {  // broadcast reads of the staged table values
+        const float* wt = win + k * 24;
+        wx = wt[ix];
+        wy0 = wt[8 + ry];
+        wy1 = wt[12 + ry];
+        const float4 z0 = *reinterpret_cast<const float4*>(wt + 16);
+        const float4 z1 = *reinterpret_cast<const float4*>(wt + 20);
+        wz[0] = z0.x, wz[1] = z0.y, wz[2] = z0.z, wz[3] = z0.w;
+        wz[4] = z1.x, wz[5] = z1.y, wz[6] = z1.z, wz[7] = z1.w;
+      } else {  // one value per lane by Horner, then shuffled
+        float W[LN::NW];
+        W[0] = lane < 24 ? P.eval(0, win[k * 4 + lane / 8]) : 0.f;
+        wx = wsel<3, 8>(W, ix);
+        wy0 = wsel<3, 8>(W, 8 + ry);
+        wy1 = wsel<3, 8>(W, 12 + ry);
 #pragma unroll
-    for (int iz = 0; iz < 8; ++iz) {
-      const float wz = wsel<3, 8>(W, 16 + iz);
-      s0r = fmaf(wz, v0[iz].x, s0r);
-      s0i = fmaf(wz, v0[iz].y, s0i);
-      s1r = fmaf(wz, v1[iz].x, s1r);
-      s1i = fmaf(wz, v1[iz].y, s1i);
-    }
-    float ar = wx * fmaf(wy0, s0r, wy1 * s1r);
-    float ai = wx * fmaf(wy0, s0i, wy1 * s1i);
+        for (int iz = 0; iz < 8; ++iz) wz[iz] = wsel<3, 8>(W, 16 + iz);
+      }
+      const float2* bp = tile + (nd.z - o2) * PLANE + (nd.y - o1 + ry) * PITCH + (nd.x - o0 + 1) + ix;
+      float2 v0[8], v1[8];
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-      ar += __shfl_xor_sync(0xFFFFFFFFu, ar, o);
-      ai += __shfl_xor_sync(0xFFFFFFFFu, ai, o);
-    }
-    if (lane == 0) fhat[nd.w] = make_float2(ar, ai);
-    nd = ndn;
+      for (int iz = 0; iz < 8; ++iz) {
+        v0[iz] = bp[iz * PLANE];
+        v1[iz] = bp[iz * PLANE + 4 * PITCH];
+      }
+      float s0r = 0.f, s0i = 0.f, s1r = 0.f, s1i = 0.f;
 #pragma unroll
-    for (int r = 0; r < LN::NW; ++r) W[r] = Wn[r];
+      for (int iz = 0; iz < 8; ++iz) {
+        s0r = fmaf(wz[iz], v0[iz].x, s0r);
+        s0i = fmaf(wz[iz], v0[iz].y, s0i);
+        s1r = fmaf(wz[iz], v1[iz].x, s1r);
+        s1i = fmaf(wz[iz], v1[iz].y, s1i);
+      }
+      ar[k] = wx * fmaf(wy0, s0r, wy1 * s1r);
+      ai[k] = wx * fmaf(wy0, s0i, wy1 * s1i);
+    }
+    // transposed reduction: after the xor-16 and xor-8 steps lane l holds
+    // node l / 8 summed over 4 lanes' worth of partials; three more steps
+    // finish it on the lanes l = 8 k
+    const bool h = (lane & 16) != 0, q = (lane & 8) != 0;
+    float a0 = (h ? ar[2] : ar[0]) + __shfl_xor_sync(0xFFFFFFFFu, h ? ar[0] : ar[2], 16);
+    float a1 = (h ? ar[3] : ar[1]) + __shfl_xor_sync(0xFFFFFFFFu, h ? ar[1] : ar[3], 16);
+    float b0 = (h ? ai[2] : ai[0]) + __shfl_xor_sync(0xFFFFFFFFu, h ? ai[0] : ai[2], 16);
+    float b1 = (h ? ai[3] : ai[1]) + __shfl_xor_sync(0xFFFFFFFFu, h ? ai[1] : ai[3], 16);
+    float sr = (q ? a1 : a0) + __shfl_xor_sync(0xFFFFFFFFu, q ? a0 : a1, 8);
+    float si = (q ? b1 : b0) + __shfl_xor_sync(0xFFFFFFFFu, q ? b0 : b1, 8);
+#pragma unroll
+    for (int o = 4; o > 0; o >>= 1) {
+      sr += __shfl_xor_sync(0xFFFFFFFFu, sr, o);
+      si += __shfl_xor_sync(0xFFFFFFFFu, si, o);
+    }
+    const int kk = lane >> 3;
+    if ((lane & 7) == 0 && base + kk < task.z) fhat[rec[kk].w] = make_float2(sr, si);
+    __syncwarp();  // the slot is read before it is staged again
+    buf ^= 1;
   }
+  asm volatile("cp.async.wait_all;" ::: "memory");
 }
 
 template <int BX, int BY, int BZ>
 int interp_tile3_launch(const nfft_plan* p, const CUtensorMap* map, const Geom<float>& G, const Nodes<float>& Nd,
                         const float2* g, float2* fhat) {
   using TC = Tile3<BX, BY, BZ>;
-  const size_t smem = TC::ACC_BYTES + 16;
+  const size_t smem =
+      TC::ACC_BYTES + 16 + (p->wtab ? Tile3Gather<true>::STAGE_BYTES : Tile3Gather<false>::STAGE_BYTES);
   auto kern = p->wtab ? interp_tile3_kernel<BX, BY, BZ, true> : interp_tile3_kernel<BX, BY, BZ, false>;
   NFFT_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
   kern<<<unsigned(p->n_tasks), kInterpThreads, smem, p->stream>>>(*map, G, Nd, p->tasks, g, fhat, p->dflag + 1);
