@@ -286,7 +286,8 @@ template <bool TABLE> struct Tile3Gather {
   static constexpr int NK = 4;
   static constexpr int WCH = TABLE ? 6 : 1;
   static constexpr int SLOT = NK * (16 + 16 * WCH);
-  static constexpr size_t STAGE_BYTES = size_t(kInterpThreads / 32) * 2 * SLOT;
+  static constexpr int NS = 2;  // (3 slots measured the same, 4 cost a CTA per SM)
+  static constexpr size_t STAGE_BYTES = size_t(kInterpThreads / 32) * NS * SLOT;
 };
 
 template <int BX, int BY, int BZ, bool TABLE>
@@ -329,8 +330,9 @@ __global__ void __launch_bounds__(kInterpThreads) interp_tile3_kernel(const __gr
   // group are copied into the warp's other stage slot by cp.async while this
   // group is summed; the first group's while the tile arrives.
   constexpr int NK = Tile3Gather<TABLE>::NK, WCH = Tile3Gather<TABLE>::WCH, SLOT = Tile3Gather<TABLE>::SLOT;
+  constexpr int NS = Tile3Gather<TABLE>::NS;
   const int ix = lane & 7, ry = lane >> 3;
-  unsigned char* stage_base = smem_raw + TC::ACC_BYTES + 16 + warp * 2 * SLOT;
+  unsigned char* stage_base = smem_raw + TC::ACC_BYTES + 16 + warp * NS * SLOT;
   auto stage = [&](int buf, int64_t gbase) {
     unsigned char* st = stage_base + buf * SLOT;
     if (lane < NK * WCH) {
@@ -347,7 +349,8 @@ __global__ void __launch_bounds__(kInterpThreads) interp_tile3_kernel(const __gr
     }
     asm volatile("cp.async.commit_group;" ::: "memory");
   };
-  stage(0, task.y + NK * warp);
+#pragma unroll
+  for (int b = 0; b + 1 < NS; ++b) stage(b, task.y + NK * warp + int64_t(b) * NK * NWARPS);
   if (threadIdx.x == 0) {
     mbar_init(mbar_s, 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -370,8 +373,8 @@ __global__ void __launch_bounds__(kInterpThreads) interp_tile3_kernel(const __gr
   }
   int buf = 0;
   for (int64_t base = task.y + NK * warp; base < task.z; base += NK * NWARPS) {
-    stage(buf ^ 1, base + NK * NWARPS);
-    asm volatile("cp.async.wait_group 1;" ::: "memory");  // this group's slot has landed
+    stage(buf == 0 ? NS - 1 : buf - 1, base + int64_t(NS - 1) * NK * NWARPS);
+    asm volatile("cp.async.wait_group %0;" ::"n"(NS - 1) : "memory");  // this group's slot has landed
     __syncwarp();
     const unsigned char* st = stage_base + buf * SLOT;
     const int4* rec = reinterpret_cast<const int4*>(st);
@@ -439,7 +442,7 @@ __global__ void __launch_bounds__(kInterpThreads) interp_tile3_kernel(const __gr
     const int kk = lane >> 3;
     if ((lane & 7) == 0 && base + kk < task.z) fhat[rec[kk].w] = make_float2(sr, si);
     __syncwarp();  // the slot is read before it is staged again
-    buf ^= 1;
+    buf = buf + 1 == NS ? 0 : buf + 1;
   }
   asm volatile("cp.async.wait_all;" ::: "memory");
 }
