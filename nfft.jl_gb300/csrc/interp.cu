@@ -333,24 +333,24 @@ __global__ void __launch_bounds__(kInterpThreads) interp_tile3_kernel(const __gr
   constexpr int NS = Tile3Gather<TABLE>::NS;
   const int ix = lane & 7, ry = lane >> 3;
   unsigned char* stage_base = smem_raw + TC::ACC_BYTES + 16 + warp * NS * SLOT;
-  auto stage = [&](int buf, int64_t gbase) {
-    unsigned char* st = stage_base + buf * SLOT;
-    if (lane < NK * WCH) {
-      const int k = lane / WCH, c = lane % WCH;
-      const int64_t id = gbase + k;
-      if (id < task.z) {
-        const float* src = TABLE ? Nd.wtab + id * 24 + 4 * c : Nd.frac4 + 4 * id;
-        cp_async_elem(reinterpret_cast<float4*>(st + NK * 16 + k * 16 * WCH + 16 * c),
-                      reinterpret_cast<const float4*>(src));
-      }
-    } else if (lane >= 24 && lane < 24 + NK) {
-      const int64_t id = gbase + (lane - 24);
-      if (id < task.z) cp_async_elem(reinterpret_cast<int4*>(st) + (lane - 24), Nd.node4 + id);
+  // this lane's copy in a stage: window chunk c of node k (lanes < NK WCH)
+  // or the record of node lane - 24 (lanes 24 .. 24 + NK - 1); node indices
+  // within a task fit in 32 bits
+  const bool win_lane = lane < NK * WCH, rec_lane = lane >= 24 && lane < 24 + NK;
+  const int cp_k = win_lane ? lane / WCH : lane - 24, cp_c = win_lane ? lane % WCH : 0;
+  const int cp_dst = win_lane ? NK * 16 + cp_k * 16 * WCH + 16 * cp_c : 16 * cp_k;
+  auto stage = [&](int buf, int gbase) {
+    const int id = gbase + cp_k;
+    if ((win_lane || rec_lane) && id < task.z) {
+      const float4* src = win_lane ? reinterpret_cast<const float4*>(TABLE ? Nd.wtab + int64_t(id) * 24 + 4 * cp_c
+                                                                              : Nd.frac4 + 4 * int64_t(id))
+                                   : reinterpret_cast<const float4*>(Nd.node4 + id);
+      cp_async_elem(reinterpret_cast<float4*>(stage_base + buf * SLOT + cp_dst), src);
     }
     asm volatile("cp.async.commit_group;" ::: "memory");
   };
 #pragma unroll
-  for (int b = 0; b + 1 < NS; ++b) stage(b, task.y + NK * warp + int64_t(b) * NK * NWARPS);
+  for (int b = 0; b + 1 < NS; ++b) stage(b, task.y + NK * warp + b * NK * NWARPS);
   if (threadIdx.x == 0) {
     mbar_init(mbar_s, 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -372,19 +372,18 @@ __global__ void __launch_bounds__(kInterpThreads) interp_tile3_kernel(const __gr
     return;
   }
   int buf = 0;
-  for (int64_t base = task.y + NK * warp; base < task.z; base += NK * NWARPS) {
-    stage(buf == 0 ? NS - 1 : buf - 1, base + int64_t(NS - 1) * NK * NWARPS);
+  // the lane's tap offset in the tile relative to a node's grid index
+  const int lane_off = ry * PITCH + ix + 1 - o0 - o1 * PITCH - o2 * PLANE;
+  for (int base = task.y + NK * warp; base < task.z; base += NK * NWARPS) {
+    stage(buf == 0 ? NS - 1 : buf - 1, base + (NS - 1) * NK * NWARPS);
     asm volatile("cp.async.wait_group %0;" ::"n"(NS - 1) : "memory");  // this group's slot has landed
     __syncwarp();
     const unsigned char* st = stage_base + buf * SLOT;
     const int4* rec = reinterpret_cast<const int4*>(st);
     const float* win = reinterpret_cast<const float*>(st + NK * 16);
     float ar[NK], ai[NK];
-#pragma unroll
-    for (int k = 0; k < NK; ++k) {
-      ar[k] = 0.f;
-      ai[k] = 0.f;
-      if (base + k >= task.z) continue;  // warp-uniform
+    // node k's partial sums (tail groups: nodes past the task end add zero)
+    auto node = [&](int k, bool valid) {
       const int4 nd = rec[k];
       // window values: x at the lane's column, y at its two rows, all 8 z
       float wx, wy0, wy1, wz[8];
@@ -406,7 +405,8 @@ __global__ void __launch_bounds__(kInterpThreads) interp_tile3_kernel(const __gr
 #pragma unroll
         for (int iz = 0; iz < 8; ++iz) wz[iz] = wsel<3, 8>(W, 16 + iz);
       }
-      const float2* bp = tile + (nd.z - o2) * PLANE + (nd.y - o1 + ry) * PITCH + (nd.x - o0 + 1) + ix;
+      // (a node past the task end reads tap 0 of the tile and is dropped)
+      const float2* bp = tile + (valid ? nd.z * PLANE + nd.y * PITCH + nd.x + lane_off : 0);
       float2 v0[8], v1[8];
 #pragma unroll
       for (int iz = 0; iz < 8; ++iz) {
@@ -421,8 +421,15 @@ __global__ void __launch_bounds__(kInterpThreads) interp_tile3_kernel(const __gr
         s1r = fmaf(wz[iz], v1[iz].x, s1r);
         s1i = fmaf(wz[iz], v1[iz].y, s1i);
       }
-      ar[k] = wx * fmaf(wy0, s0r, wy1 * s1r);
-      ai[k] = wx * fmaf(wy0, s0i, wy1 * s1i);
+      ar[k] = valid ? wx * fmaf(wy0, s0r, wy1 * s1r) : 0.f;
+      ai[k] = valid ? wx * fmaf(wy0, s0i, wy1 * s1i) : 0.f;
+    };
+    if (base + NK <= task.z) {
+#pragma unroll
+      for (int k = 0; k < NK; ++k) node(k, true);
+    } else {
+#pragma unroll
+      for (int k = 0; k < NK; ++k) node(k, base + k < task.z);
     }
     // transposed reduction: after the xor-16 and xor-8 steps lane l holds
     // node l / 8 summed over 4 lanes' worth of partials; three more steps
