@@ -263,21 +263,6 @@ __global__ void __launch_bounds__(kInterpThreads) interp_tile_kernel(Geom<T> G, 
 // interp_kernel does.  The wait for the copy is bounded: on timeout the CTA
 // raises status word 1 (reported by nfft_sync) and skips its nodes.
 
-__device__ __forceinline__ void mbar_init(unsigned addr, unsigned count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(addr), "r"(count) : "memory");
-}
-__device__ __forceinline__ void mbar_expect_tx(unsigned addr, unsigned bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(addr), "r"(bytes) : "memory");
-}
-__device__ __forceinline__ bool mbar_try_wait(unsigned addr, unsigned parity) {
-  unsigned ok;
-  asm volatile(
-      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
-      : "=r"(ok)
-      : "r"(addr), "r"(parity)
-      : "memory");
-  return ok != 0;
-}
 
 // Per-warp staging of the TMA gather: NK nodes per group, WCH 16-byte chunks
 // of window data per node (24 table values, or the 4 fractional offsets),

@@ -36,6 +36,23 @@ template <int BX, int BY, int BZ> struct Tile3 {
   static_assert(PITCH <= 128 && P1 <= 256 && P2 <= 256, "TMA box extents");
 };
 
+// mbarrier operations on a shared-memory barrier at address addr.
+__device__ __forceinline__ void mbar_init(unsigned addr, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(addr), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(unsigned addr, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(addr), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(unsigned addr, unsigned parity) {
+  unsigned ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+      : "=r"(ok)
+      : "r"(addr), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
 // The grid region of a tile's padded box lies inside the grid (no wrap):
 // the box is added with one bulk tensor reduction.
 template <int BX, int BY, int BZ>
