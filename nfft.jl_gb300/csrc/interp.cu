@@ -280,7 +280,8 @@ __global__ void __launch_bounds__(kInterpThreads) interp_tile3_kernel(const __gr
                                                                        Geom<float> G, Nodes<float> Nd,
                                                                        const int4* __restrict__ tasks,
                                                                        const float2* __restrict__ g,
-                                                                       float2* __restrict__ fhat, int* status) {
+                                                                       float2* __restrict__ fhat, int* status,
+                                                                       int pf_dist) {
   using TC = Tile3<BX, BY, BZ>;
   using LN = Lanes<3, 8>;
   constexpr int PITCH = TC::PITCH, PLANE = TC::PLANE;
@@ -348,6 +349,20 @@ __global__ void __launch_bounds__(kInterpThreads) interp_tile3_kernel(const __gr
         "[%5];" ::"r"(tile_s),
         "l"(reinterpret_cast<uint64_t>(&tmap)), "r"(2 * (q0 - 4)), "r"(q1 - 3), "r"(q2 - 3), "r"(mbar_s)
         : "memory");
+  } else if (threadIdx.x == 32 && pf_dist > 0 && blockIdx.x + unsigned(pf_dist) < gridDim.x) {
+    // the tile of the task about one wave of resident CTAs ahead, fetched
+    // into L2 now so that its CTA's bulk copy need not wait on DRAM
+    const int tn = tasks[blockIdx.x + pf_dist].x;
+    if (tn != t) {
+      const int p0 = wrap_once((tn % G.ntiles[0]) * BX + G.sh[0], G.Nt[0]);
+      const int p1 = wrap_once(((tn / G.ntiles[0]) % G.ntiles[1]) * BY + G.sh[1], G.Nt[1]);
+      const int p2 = wrap_once((tn / (G.ntiles[0] * G.ntiles[1])) * BZ + G.sh[2], G.Nt[2]);
+      if (tile3_interior<BX, BY, BZ>(G, p0, p1, p2))
+        asm volatile("cp.async.bulk.prefetch.tensor.3d.L2.global.tile [%0, {%1, %2, %3}];" ::"l"(
+                         reinterpret_cast<uint64_t>(&tmap)),
+                     "r"(2 * (p0 - 4)), "r"(p1 - 3), "r"(p2 - 3)
+                     : "memory");
+    }
   }
   bool done = false;
   for (int it = 0; it < (1 << 22) && !done; ++it) done = mbar_try_wait(mbar_s, 0);
@@ -447,7 +462,11 @@ int interp_tile3_launch(const nfft_plan* p, const CUtensorMap* map, const Geom<f
       TC::ACC_BYTES + 16 + (p->wtab ? Tile3Gather<true>::STAGE_BYTES : Tile3Gather<false>::STAGE_BYTES);
   auto kern = p->wtab ? interp_tile3_kernel<BX, BY, BZ, true> : interp_tile3_kernel<BX, BY, BZ, false>;
   NFFT_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
-  kern<<<unsigned(p->n_tasks), kInterpThreads, smem, p->stream>>>(*map, G, Nd, p->tasks, g, fhat, p->dflag + 1);
+  int dev = 0, sms = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+    sms = 0;
+  kern<<<unsigned(p->n_tasks), kInterpThreads, smem, p->stream>>>(*map, G, Nd, p->tasks, g, fhat, p->dflag + 1,
+                                                                   p->gather_pf * sms);
   NFFT_LAUNCH_CHECK();
   return NFFT_OK;
 }
