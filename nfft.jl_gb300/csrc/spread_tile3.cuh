@@ -39,7 +39,7 @@ __global__ void __launch_bounds__(256) spread_tile3_kernel(const __grid_constant
   fsorted += blockIdx.y * fcol;  // column of a multi-column launch
   g += blockIdx.y * gcol;
   float2* acc = reinterpret_cast<float2*>(smem_raw);
-  int4* s_meta = reinterpret_cast<int4*>(smem_raw + TC::ACC_BYTES);  // {row/column offset, z offset}
+  int4* s_meta = reinterpret_cast<int4*>(smem_raw + TC::ACC_BYTES);  // [NB] {tap offset, z plane}
   float2* s_c = reinterpret_cast<float2*>(s_meta + NB);                // [NB]
   float2* s_cz = s_c + NB;                                             // [NB][L]: value x z window value
   float* s_w = reinterpret_cast<float*>(s_cz + NB * L);                // [NB][3L]
@@ -84,7 +84,9 @@ __global__ void __launch_bounds__(256) spread_tile3_kernel(const __grid_constant
     const int n = min(NB, task.z - b);
     // stage 1: registers -> shared (window values evaluated here for POLYNOMIAL)
     if (threadIdx.x < n) {
-      s_meta[threadIdx.x] = make_int4((r_nd.y - o1) * PITCH + (r_nd.x - o0 + 1), r_nd.z - o2, 0, 0);
+      // {offset of the window's first tap in the padded tile, its z plane}
+      const int z0 = r_nd.z - o2;
+      s_meta[threadIdx.x] = make_int4(z0 * PLANE + (r_nd.y - o1) * PITCH + (r_nd.x - o0 + 1), z0, 0, 0);
       s_c[threadIdx.x] = r_c;
     }
 #pragma unroll
@@ -104,7 +106,9 @@ __global__ void __launch_bounds__(256) spread_tile3_kernel(const __grid_constant
       }
     }
     __syncthreads();
-    // stage 2: thread (node s, row iy): the row of x-y products and c * wz[iy]
+    // stage 2: thread (node s, row iy): the row of x-y products, and for
+    // warp iy the value times the z window value of the slice it owns,
+    // c * wz[(iy - z0) mod 8]
     {
       const int s = threadIdx.x >> 3, iy = threadIdx.x & 7;
       if (s < n) {
@@ -115,7 +119,7 @@ __global__ void __launch_bounds__(256) spread_tile3_kernel(const __grid_constant
         float4* out = reinterpret_cast<float4*>(s_xy + s * L * L + iy * L);
         out[0] = make_float4(x0.x * wyv, x0.y * wyv, x0.z * wyv, x0.w * wyv);
         out[1] = make_float4(x1.x * wyv, x1.y * wyv, x1.z * wyv, x1.w * wyv);
-        const float wz = ws[2 * L + iy];
+        const float wz = ws[2 * L + ((iy - s_meta[s].y) & 7)];
         const float2 c = s_c[s];
         s_cz[s * L + iy] = make_float2(c.x * wz, c.y * wz);
       }
@@ -125,12 +129,12 @@ __global__ void __launch_bounds__(256) spread_tile3_kernel(const __grid_constant
     // taps: warp w updates its slice of every node, rows iy and iy + 4 of the
     // lane's column; the next node's record is loaded during this node's taps
     int4 mt = s_meta[0];
+    float2* const accl = acc + lofs;
     for (int s = 0; s < n; ++s) {
-      const int4 mn = s_meta[s + 1 < n ? s + 1 : s];
-      const int is = (warp - mt.y) & 7;
-      float2* p = acc + (mt.y + is) * PLANE + mt.x + lofs;
+      const int4 mn = s_meta[s + 1];  // (past the last node: a value in s_c, unused)
+      float2* p = accl + mt.x + ((warp - mt.y) & 7) * PLANE;
       const float* xy = s_xy + s * L * L + lane;
-      const float2 cz = s_cz[s * L + is];
+      const float2 cz = s_cz[s * L + warp];
       float2 a0 = p[0], a1 = p[4 * PITCH];
       const float w0 = xy[0], w1 = xy[32];
       a0.x = fmaf(cz.x, w0, a0.x);
