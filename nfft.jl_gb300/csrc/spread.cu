@@ -61,9 +61,18 @@ int tile3_launch(nfft_plan* p, const Geom<float>& G, const Nodes<float>& Nd, con
   using TC = Tile3<BX, BY, BZ>;
   const CUtensorMap* map = (ncols == 1 && p->spread_tma) ? tile3_map<BX, BY, BZ>(p, gp) : nullptr;
   const int use_tma = map ? 1 : 0;
+  CUtensorMap none{};
+  if (p->wtab && p->spread_rec) {  // window values from the table: one-step staging
+    using TR = Tile3Rec<BX, BY, BZ>;
+    auto kr = spread_tile3_rec_kernel<BX, BY, BZ>;
+    NFFT_CUDA_TRY(cudaFuncSetAttribute(kr, cudaFuncAttributeMaxDynamicSharedMemorySize, int(TR::SMEM)));
+    kr<<<dim3(unsigned(p->n_tasks), unsigned(ncols)), TC::THREADS, TR::SMEM, p->stream>>>(
+        map ? *map : none, use_tma, G, Nd, p->tasks, fs, gp, ncols > 1 ? fcol : 0, gcol_t);
+    NFFT_LAUNCH_CHECK();
+    return NFFT_OK;
+  }
   auto kern = p->wtab ? spread_tile3_kernel<BX, BY, BZ, true> : spread_tile3_kernel<BX, BY, BZ, false>;
   NFFT_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(TC::SMEM)));
-  CUtensorMap none{};
   kern<<<dim3(unsigned(p->n_tasks), unsigned(ncols)), TC::THREADS, TC::SMEM, p->stream>>>(
       map ? *map : none, use_tma, G, Nd, p->tasks, fs, gp, ncols > 1 ? fcol : 0, gcol_t);
   NFFT_LAUNCH_CHECK();

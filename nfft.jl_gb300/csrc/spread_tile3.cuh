@@ -173,5 +173,131 @@ __global__ void __launch_bounds__(256) spread_tile3_kernel(const __grid_constant
   flush_tile<3, float, false, 8>(G, acc + 1, g, o0, o1, o2, TC::P0 - 1, TC::P1, TC::P2, PITCH);
 }
 
+// Variant for window values from the table with one staging step: thread
+// (node s, row iy) of a batch loads the node's record, value and window
+// values itself (a batch ahead, in registers) and writes row iy of the x-y
+// products and the 16-byte record of owner warp iy: {offset of the warp's
+// first tap in the padded tile, value x z window value of its slice}.  The
+// tap loop then reads one broadcast record per node instead of a node record
+// and a slice value, and the staging needs neither a window-value area nor a
+// second CTA barrier: ~11 instead of ~15 shared-memory wavefronts per node
+// and warp outside the taps' read-modify-writes.
+template <int BX, int BY, int BZ> struct Tile3Rec {
+  using TC = Tile3<BX, BY, BZ>;
+  static constexpr int NB = 32;
+  static constexpr size_t REC_BYTES = size_t(NB) * 8 * 16;  // float4 [NB][8 warps]
+  static constexpr size_t SMEM = TC::ACC_BYTES + REC_BYTES + size_t(NB) * 64 * 4;
+};
+
+template <int BX, int BY, int BZ>
+__global__ void __launch_bounds__(256, 4) spread_tile3_rec_kernel(const __grid_constant__ CUtensorMap tmap, int use_tma,
+                                                                Geom<float> G, Nodes<float> Nd,
+                                                                const int4* __restrict__ tasks,
+                                                                const float2* __restrict__ fsorted,
+                                                                float* __restrict__ g, int64_t fcol, int64_t gcol) {
+  using TC = Tile3<BX, BY, BZ>;
+  using TR = Tile3Rec<BX, BY, BZ>;
+  constexpr int NB = TR::NB, PITCH = TC::PITCH, PLANE = TC::PLANE;
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  fsorted += blockIdx.y * fcol;  // column of a multi-column launch
+  g += blockIdx.y * gcol;
+  float2* acc = reinterpret_cast<float2*>(smem_raw);
+  float4* s_rec = reinterpret_cast<float4*>(smem_raw + TC::ACC_BYTES);        // [NB][8]
+  float* s_xy = reinterpret_cast<float*>(smem_raw + TC::ACC_BYTES + TR::REC_BYTES);  // [NB][64]
+  const int4 task = tasks[blockIdx.x];
+  const int tile = task.x;
+  const int tc0 = tile % G.ntiles[0];
+  const int tc1 = (tile / G.ntiles[0]) % G.ntiles[1];
+  const int tc2 = tile / (G.ntiles[0] * G.ntiles[1]);
+  const int o0 = tc0 * BX, o1 = tc1 * BY, o2 = tc2 * BZ;
+  {
+    float4* a4 = reinterpret_cast<float4*>(acc);
+    for (int q = threadIdx.x; q < TC::NACC / 2; q += TC::THREADS) a4[q] = make_float4(0.f, 0.f, 0.f, 0.f);
+  }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int s = threadIdx.x >> 3, iy = threadIdx.x & 7, hsel = (iy >> 2) & 1;
+
+  // register prefetch of this thread's node of one batch
+  int4 r_nd = make_int4(0, 0, 0, 0);
+  float2 r_c = make_float2(0.f, 0.f);
+  float4 r_x0 = make_float4(0.f, 0.f, 0.f, 0.f), r_x1 = r_x0, r_z0 = r_x0, r_z1 = r_x0;
+  float r_y = 0.f;
+  auto prefetch = [&](int b) {
+    const int j = b + s;
+    if (j < task.z) {
+      const float* wt = Nd.wtab + int64_t(j) * 24;
+      r_nd = __ldg(Nd.node4 + j);
+      r_c = __ldg(fsorted + j);
+      r_x0 = __ldg(reinterpret_cast<const float4*>(wt));
+      r_x1 = __ldg(reinterpret_cast<const float4*>(wt + 4));
+      r_y = __ldg(wt + 8 + iy);
+      r_z0 = __ldg(reinterpret_cast<const float4*>(wt + 16));
+      r_z1 = __ldg(reinterpret_cast<const float4*>(wt + 20));
+    }
+  };
+  if (task.y < task.z) prefetch(task.y);
+  __syncthreads();
+
+  float2* const accl = acc + (lane >> 3) * PITCH + (lane & 7);  // this lane's tap (x = lane mod 8, row = lane / 8)
+  for (int b = task.y; b < task.z; b += NB) {
+    const int n = min(NB, task.z - b);
+    if (s < n) {
+      // the record of owner warp iy: its slice is = (iy - z0) mod 8 of the window
+      const int z0 = r_nd.z - o2;
+      const int is = (iy - z0) & 7;
+      const float wz = is < 4 ? (is < 2 ? (is == 0 ? r_z0.x : r_z0.y) : (is == 2 ? r_z0.z : r_z0.w))
+                              : (is < 6 ? (is == 4 ? r_z1.x : r_z1.y) : (is == 6 ? r_z1.z : r_z1.w));
+      const int off = (z0 + is) * PLANE + (r_nd.y - o1) * PITCH + (r_nd.x - o0 + 1);
+      s_rec[s * 8 + iy] = make_float4(__int_as_float(off), 0.f, r_c.x * wz, r_c.y * wz);
+      // row iy of the x-y products; the two halves in an order that keeps
+      // the eight lanes of each 128-bit store phase on distinct banks
+      float4* out = reinterpret_cast<float4*>(s_xy + s * 64 + iy * 8);
+      const float4 xa = hsel ? r_x1 : r_x0, xb = hsel ? r_x0 : r_x1;
+      out[hsel] = make_float4(xa.x * r_y, xa.y * r_y, xa.z * r_y, xa.w * r_y);
+      out[hsel ^ 1] = make_float4(xb.x * r_y, xb.y * r_y, xb.z * r_y, xb.w * r_y);
+    }
+    __syncthreads();
+    if (b + NB < task.z) prefetch(b + NB);
+    // taps: warp w updates its slice of every node, rows iy and iy + 4 of the
+    // lane's column; the next node's record is loaded during this node's taps
+    float4 rt = s_rec[warp];
+    for (int q = 0; q < n; ++q) {
+      const float4 rn = s_rec[(q + 1) * 8 + warp];  // (past the last node: in-bounds, unused)
+      float2* p = accl + __float_as_int(rt.x);
+      const float* xy = s_xy + q * 64 + lane;
+      float2 a0 = p[0], a1 = p[4 * PITCH];
+      const float w0 = xy[0], w1 = xy[32];
+      a0.x = fmaf(rt.z, w0, a0.x);
+      a0.y = fmaf(rt.w, w0, a0.y);
+      a1.x = fmaf(rt.z, w1, a1.x);
+      a1.y = fmaf(rt.w, w1, a1.y);
+      p[0] = a0;
+      p[4 * PITCH] = a1;
+      rt = rn;
+    }
+    __syncthreads();
+  }
+  // the tile's shared-memory writes, made visible to the bulk (async) copy
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  __syncthreads();
+  const int q0 = wrap_once(o0 + G.sh[0], G.Nt[0]), q1 = wrap_once(o1 + G.sh[1], G.Nt[1]);
+  const int q2 = wrap_once(o2 + G.sh[2], G.Nt[2]);
+  if (use_tma && tile3_interior<BX, BY, BZ>(G, q0, q1, q2) &&
+      (static_cast<unsigned>(__cvta_generic_to_shared(acc)) & 127u) == 0) {
+    if (threadIdx.x == 0) {
+      const int x = 2 * (q0 - 4), y = q1 - 3, z = q2 - 3;  // x in floats: a multiple of 4 (16 bytes)
+      const unsigned src = static_cast<unsigned>(__cvta_generic_to_shared(acc));
+      asm volatile(
+          "cp.reduce.async.bulk.tensor.3d.global.shared::cta.add.tile.bulk_group [%0, {%1, %2, %3}], [%4];"
+          ::"l"(reinterpret_cast<uint64_t>(&tmap)), "r"(x), "r"(y), "r"(z), "r"(src)
+          : "memory");
+      asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+      asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");  // the tile has been read before exit
+    }
+    return;
+  }
+  flush_tile<3, float, false, 8>(G, acc + 1, g, o0, o1, o2, TC::P0 - 1, TC::P1, TC::P2, PITCH);
+}
+
 }  // namespace
 }  // namespace nfft

@@ -321,15 +321,18 @@ def test_paper_accuracy_d2_tensor_gpu_fp64():
 
 @pytest.mark.parametrize("bs", [(16, 8, 8), (16, 16, 8), (32, 8, 8), (8, 8, 8)])
 @pytest.mark.parametrize("pre", [oracle.TENSOR, oracle.POLYNOMIAL])
-@pytest.mark.parametrize("path", ["tma", "points", "generic"])
+@pytest.mark.parametrize("path", ["tma", "points", "generic", "tma-two-step", "points-two-step"])
 def test_specialised_3d_spreader(monkeypatch, bs, pre, path):
     """The shape-specialised 3-D FP32 m = 4 spreader, with the bulk tensor
     reduction flush for tiles inside the grid ("tma"), with the per-point
     flush only ("points"), and the generic kernel ("generic"), all give the
-    oracle's adjoint; the grid has interior tiles and tiles that wrap in every
-    dimension, boundary nodes included."""
+    oracle's adjoint; table windows run the one-step staging with per-warp
+    records by default and the two-step staging with
+    NFFT_GB300_SPREAD_REC=0 ("-two-step").  The grid has interior tiles and
+    tiles that wrap in every dimension, boundary nodes included."""
     monkeypatch.setenv("NFFT_GB300_SPREAD_TILE3", "0" if path == "generic" else "1")
-    monkeypatch.setenv("NFFT_GB300_SPREAD_TMA", "1" if path == "tma" else "0")
+    monkeypatch.setenv("NFFT_GB300_SPREAD_TMA", "1" if path.startswith("tma") else "0")
+    monkeypatch.setenv("NFFT_GB300_SPREAD_REC", "0" if path.endswith("two-step") else "1")
     N = (48, 40, 36)
     k, f, fhat = rand_problem(3, N, 30000, seed=300, dtype=np.float32)
     k[:, :5] = np.array([[-0.5, 0.4999, 0.0, -0.001, 0.25]] * 3, dtype=np.float32)
