@@ -616,6 +616,83 @@ __global__ void __launch_bounds__(256, FWD ? 3 : 2) fft4_lines_kernel(LineGeom L
   }
 }
 
+// The same four-step line FFT with the CTA's W x NL tile staged in shared
+// memory first: every thread issues its share of 16-byte cp.async copies of
+// the tile at once (the forward copies only the image rows), so a CTA has
+// its whole tile in flight without holding it in registers.  The tile is
+// row-major [position][W columns] without padding and the FFT runs in place:
+// the R1-point DFTs of column w, offset n2 write their outputs to the rows
+// they read (row R2 k1 + n2), and the R2-point DFTs of k1 read rows
+// R2 k1 .. R2 k1 + R2 - 1; half-warps cover the 16 columns of one row in every
+// access, so no access has a bank conflict.  W x NL x 8 bytes of shared
+// memory (64 KB at NL = 512).
+template <int NL, bool FWD>
+__global__ void __launch_bounds__(256, 3) fft4_lines_staged_kernel(LineGeom L, float2* __restrict__ g,
+                                                                   const float2* __restrict__ tw) {
+  using C = float2;
+  constexpr int R1 = Split4<NL>::R1, R2 = Split4<NL>::R2, W = kW4, S = FWD ? -1 : 1;
+  static_assert(W == 16, "a row of the tile is 8 16-byte chunks");
+  extern __shared__ __align__(16) unsigned char fft_smem[];
+  C* buf = reinterpret_cast<C*>(fft_smem);
+  const int tile = blockIdx.x % L.tiles_x;
+  const int o = blockIdx.x / L.tiles_x;
+  const int go = L.outer_N > 0 ? wrap_once(o - L.outer_N / 2, L.outer_Nt) : o;
+  C* base = g + int64_t(go) * L.outer_stride + int64_t(tile) * W;
+  const int head = L.n_img - L.n_img / 2, tail0 = NL - L.n_img / 2;
+  // stage the tile: NL rows of W complex values (8 chunks of 16 bytes)
+  for (int c = threadIdx.x; c < NL * 8; c += 256) {
+    const int row = c >> 3, part = c & 7;
+    if (!FWD || row < head || row >= tail0) {
+      const unsigned dst = static_cast<unsigned>(__cvta_generic_to_shared(buf + row * W + 2 * part));
+      asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst),
+                   "l"(base + int64_t(row) * L.stride + 2 * part)
+                   : "memory");
+    }
+  }
+  asm volatile("cp.async.wait_all;" ::: "memory");
+  __syncthreads();
+  // R1-point DFTs in place: thread (w, n2) owns rows R2 n1 + n2 of column w
+  constexpr int T1 = W * R2, B1 = (T1 + 255) / 256;
+#pragma unroll
+  for (int b = 0; b < B1; ++b) {
+    const int task = int(threadIdx.x) + b * 256;
+    if (T1 % 256 == 0 || task < T1) {
+      const int w = task % W, n2 = task / W;
+      C v[R1];
+#pragma unroll
+      for (int n1 = 0; n1 < R1; ++n1) {
+        const int n = R2 * n1 + n2;
+        v[n1].x = 0.f;
+        v[n1].y = 0.f;
+        if (!FWD || n < head || n >= tail0) v[n1] = buf[n * W + w];
+      }
+      dft_reg<S, R1>(v);
+      twiddle4<S, NL, R1>(v, n2, tw);
+#pragma unroll
+      for (int k1 = 0; k1 < R1; ++k1) buf[(R2 * k1 + n2) * W + w] = v[k1];
+    }
+  }
+  __syncthreads();
+  // R2-point DFTs: thread (w, k1) reads rows R2 k1 .. R2 k1 + R2 - 1
+  constexpr int T2 = W * R1, B2 = (T2 + 255) / 256;
+#pragma unroll
+  for (int b = 0; b < B2; ++b) {
+    const int task = int(threadIdx.x) + b * 256;
+    if (T2 % 256 == 0 || task < T2) {
+      const int w = task % W, k1 = task / W;
+      C v[R2];
+#pragma unroll
+      for (int n2 = 0; n2 < R2; ++n2) v[n2] = buf[(R2 * k1 + n2) * W + w];
+      dft_reg<S, R2>(v);
+#pragma unroll
+      for (int k2 = 0; k2 < R2; ++k2) {
+        const int pos = k1 + R1 * k2;
+        if (FWD || pos < head || pos >= tail0) base[w + int64_t(pos) * L.stride] = v[k2];
+      }
+    }
+  }
+}
+
 // x lines of the image rows: forward pad + deconvolution + FFT (FWD), or
 // backward FFT + crop + deconvolution.
 template <int NX, bool FWD>
@@ -907,6 +984,14 @@ template <typename T, int NL> int line_pass_t(nfft_plan* p, int axis, bool fwd) 
   if constexpr (sizeof(T) == 4 && NL <= 512 && NFFT_FFT_FOURSTEP) {
     const LineGeom L = make_line_geom(p, axis, kW4, &outer_count);
     const unsigned blocks4 = unsigned(outer_count * L.tiles_x);
+    if (p->fft_staged) {  // tile staged by cp.async, in-place four-step
+      const size_t smem_s = size_t(NL) * kW4 * sizeof(float2);
+      auto ks = fwd ? fft4_lines_staged_kernel<NL, true> : fft4_lines_staged_kernel<NL, false>;
+      if (int rc = set_smem(ks, smem_s)) return rc;
+      ks<<<blocks4, 256, smem_s, p->stream>>>(L, g, tw);
+      NFFT_LAUNCH_CHECK();
+      return NFFT_OK;
+    }
     const size_t smem4 = fft4_smem_bytes<NL>();
     auto kern = fwd ? fft4_lines_kernel<NL, true> : fft4_lines_kernel<NL, false>;
     if (int rc = set_smem(kern, smem4)) return rc;

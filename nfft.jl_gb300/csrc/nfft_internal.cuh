@@ -162,6 +162,7 @@ struct nfft_plan {
   cudaStream_t zero_stream = nullptr;
   cudaEvent_t ev_grid2_used = nullptr, ev_grid2_zeroed = nullptr;
   bool skip_memset = false;
+  bool fft_staged = true;          // FP32 line FFTs: tile staged by cp.async, in-place four-step
   bool spread_rec = true;          // 3-D FP32 table spreader: one-step staging with per-warp records
   int gather_pf = 4;               // TMA gather: L2 prefetch of the tile gather_pf x (SM count) tasks ahead (0: off)        // set while the spreading target is known to be zero
   int gather_pitch = 0;            // shared-memory row pitch of the staged gather tile

@@ -562,6 +562,7 @@ int nfft_plan_create(nfft_plan** out, int precision, int D, const int64_t* N, in
   if (const char* e = getenv("NFFT_GB300_CENTER")) p->center = e[0] != '0';
   // the adjoint's pre-zeroed second grid (on by default)
   if (const char* e = getenv("NFFT_GB300_PREZERO")) p->prezero = e[0] != '0';
+  if (const char* e = getenv("NFFT_GB300_FFT_STAGED")) p->fft_staged = e[0] != '0';
   if (const char* e = getenv("NFFT_GB300_SPREAD_REC")) p->spread_rec = e[0] != '0';
   if (const char* e = getenv("NFFT_GB300_GATHER_PF")) p->gather_pf = std::max(0, std::min(64, atoi(e)));
   p->ntiles_total = 1;

@@ -190,13 +190,17 @@ FUSED_CASES = [
 
 @pytest.mark.parametrize("N,sigma", FUSED_CASES)
 @pytest.mark.parametrize("prec", [64, 32])
-def test_fused_fft_matches_oracle_and_cufft(N, sigma, prec, monkeypatch):
+@pytest.mark.parametrize("staged", ["1", "0"])
+def test_fused_fft_matches_oracle_and_cufft(N, sigma, prec, staged, monkeypatch):
     """The fused pad/deconvolve + pruned FFT (and pruned inverse FFT + crop)
-    against the oracle and against the same plan on cuFFT."""
+    against the oracle and against the same plan on cuFFT; FP32 lines run
+    with the tile staged in shared memory (default) and from registers
+    (NFFT_GB300_FFT_STAGED=0)."""
     dtype = np.float64 if prec == 64 else np.float32
     D = len(N)
     M = 3000
     k, f, fhat = rand_problem(D, N, M, seed=77 + D, dtype=dtype)
+    monkeypatch.setenv("NFFT_GB300_FFT_STAGED", staged)
     p = nf.plan_nfft(k, N, m=4, sigma=sigma, precompute=oracle.TENSOR)
     assert all(n & (n - 1) == 0 for n in p.Ñ)
     monkeypatch.setenv("NFFT_GB300_FFT", "cufft")
