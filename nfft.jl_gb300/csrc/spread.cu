@@ -62,21 +62,44 @@ int tile3_launch(nfft_plan* p, const Geom<float>& G, const Nodes<float>& Nd, con
   const CUtensorMap* map = (ncols == 1 && p->spread_tma) ? tile3_map<BX, BY, BZ>(p, gp) : nullptr;
   const int use_tma = map ? 1 : 0;
   CUtensorMap none{};
-  if (p->wtab && p->spread_rec) {  // window values from the table: one-step staging
-    using TR = Tile3Rec<BX, BY, BZ>;
-    auto kr = spread_tile3_rec_kernel<BX, BY, BZ>;
-    NFFT_CUDA_TRY(cudaFuncSetAttribute(kr, cudaFuncAttributeMaxDynamicSharedMemorySize, int(TR::SMEM)));
-    kr<<<dim3(unsigned(p->n_tasks), unsigned(ncols)), TC::THREADS, TR::SMEM, p->stream>>>(
-        map ? *map : none, use_tma, G, Nd, p->tasks, fs, gp, ncols > 1 ? fcol : 0, gcol_t);
-    NFFT_LAUNCH_CHECK();
-    return NFFT_OK;
-  }
   auto kern = p->wtab ? spread_tile3_kernel<BX, BY, BZ, true> : spread_tile3_kernel<BX, BY, BZ, false>;
   NFFT_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(TC::SMEM)));
   kern<<<dim3(unsigned(p->n_tasks), unsigned(ncols)), TC::THREADS, TC::SMEM, p->stream>>>(
       map ? *map : none, use_tma, G, Nd, p->tasks, fs, gp, ncols > 1 ? fcol : 0, gcol_t);
   NFFT_LAUNCH_CHECK();
   return NFFT_OK;
+}
+
+// The one-step staging kernel for table windows: values fhat + c fcol in the
+// caller's order, read through the bin-sorted nodes' input indices.
+template <int BX, int BY, int BZ>
+int tile3_rec_launch(nfft_plan* p, const Geom<float>& G, const Nodes<float>& Nd, const float2* fhat, float* gp,
+                     int ncols, int64_t fcol, int64_t gcol_t) {
+  using TC = Tile3<BX, BY, BZ>;
+  using TR = Tile3Rec<BX, BY, BZ>;
+  const CUtensorMap* map = (ncols == 1 && p->spread_tma) ? tile3_map<BX, BY, BZ>(p, gp) : nullptr;
+  CUtensorMap none{};
+  auto kr = spread_tile3_rec_kernel<BX, BY, BZ>;
+  NFFT_CUDA_TRY(cudaFuncSetAttribute(kr, cudaFuncAttributeMaxDynamicSharedMemorySize, int(TR::SMEM)));
+  kr<<<dim3(unsigned(p->n_tasks), unsigned(ncols)), TC::THREADS, TR::SMEM, p->stream>>>(
+      map ? *map : none, map ? 1 : 0, G, Nd, p->tasks, fhat, gp, ncols > 1 ? fcol : 0, gcol_t);
+  NFFT_LAUNCH_CHECK();
+  return NFFT_OK;
+}
+
+// The one-step kernel when the plan's tiles have a shape-specialised form and
+// its window values come from the table (no value sort); -1 = not applicable.
+int spread_tile3_user(nfft_plan* p, const Geom<float>& G, const Nodes<float>& Nd, const float2* fhat, float* gp,
+                      int ncols, int64_t fcol, int64_t gcol_t) {
+  if (!p->spread_tile3 || !p->spread_rec || !p->wtab || p->D != 3 || p->m != 4 || p->prm.compensated ||
+      p->spread_layout != 1 || p->bs[2] != 8)
+    return -1;
+  const int64_t bx = p->bs[0], by = p->bs[1];
+  if (bx == 16 && by == 8) return tile3_rec_launch<16, 8, 8>(p, G, Nd, fhat, gp, ncols, fcol, gcol_t);
+  if (bx == 16 && by == 16) return tile3_rec_launch<16, 16, 8>(p, G, Nd, fhat, gp, ncols, fcol, gcol_t);
+  if (bx == 32 && by == 8) return tile3_rec_launch<32, 8, 8>(p, G, Nd, fhat, gp, ncols, fcol, gcol_t);
+  if (bx == 8 && by == 8) return tile3_rec_launch<8, 8, 8>(p, G, Nd, fhat, gp, ncols, fcol, gcol_t);
+  return -1;
 }
 
 // The shape-specialised 3-D kernel when the plan's tiles have one of its
@@ -150,6 +173,10 @@ int spread_launch(nfft_plan* p, const void* fhat, void* g, int ncols, int64_t fc
         kern = p->wtab ? spread_owned_kernel<D, L, T, true, false, 2> : spread_owned_kernel<D, L, T, false, false, 2>;
         threads = OwnedCfg<D, L, 2>::THREADS;
       }
+    }
+    if constexpr (D == 3 && L == 8 && sizeof(T) == 4) {  // values read in the caller's order
+      const int rc = spread_tile3_user(p, G, Nd, fp, gp, ncols, fcol, gcol_t);
+      if (rc != -1) return rc;
     }
     NFFT_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
     C* fs = static_cast<C*>(ncols > 1 ? sorted : p->fsorted);

@@ -174,8 +174,9 @@ __global__ void __launch_bounds__(256) spread_tile3_kernel(const __grid_constant
 }
 
 // Variant for window values from the table with one staging step: thread
-// (node s, row iy) of a batch loads the node's record, value and window
-// values itself (a batch ahead, in registers) and writes row iy of the x-y
+// (node s, row iy) of a batch loads the node's record, value (from the
+// caller's order through the node's input index: no separate value sort)
+// and window values itself (a batch ahead, in registers) and writes row iy of the x-y
 // products and the 16-byte record of owner warp iy: {offset of the warp's
 // first tap in the padded tile, value x z window value of its slice}.  The
 // tap loop then reads one broadcast record per node instead of a node record
@@ -193,13 +194,13 @@ template <int BX, int BY, int BZ>
 __global__ void __launch_bounds__(256, 4) spread_tile3_rec_kernel(const __grid_constant__ CUtensorMap tmap, int use_tma,
                                                                 Geom<float> G, Nodes<float> Nd,
                                                                 const int4* __restrict__ tasks,
-                                                                const float2* __restrict__ fsorted,
+                                                                const float2* __restrict__ fhat,
                                                                 float* __restrict__ g, int64_t fcol, int64_t gcol) {
   using TC = Tile3<BX, BY, BZ>;
   using TR = Tile3Rec<BX, BY, BZ>;
   constexpr int NB = TR::NB, PITCH = TC::PITCH, PLANE = TC::PLANE;
   extern __shared__ __align__(1024) unsigned char smem_raw[];
-  fsorted += blockIdx.y * fcol;  // column of a multi-column launch
+  fhat += blockIdx.y * fcol;  // column of a multi-column launch
   g += blockIdx.y * gcol;
   float2* acc = reinterpret_cast<float2*>(smem_raw);
   float4* s_rec = reinterpret_cast<float4*>(smem_raw + TC::ACC_BYTES);        // [NB][8]
@@ -227,7 +228,7 @@ __global__ void __launch_bounds__(256, 4) spread_tile3_rec_kernel(const __grid_c
     if (j < task.z) {
       const float* wt = Nd.wtab + int64_t(j) * 24;
       r_nd = __ldg(Nd.node4 + j);
-      r_c = __ldg(fsorted + j);
+      r_c = __ldg(fhat + r_nd.w);
       r_x0 = __ldg(reinterpret_cast<const float4*>(wt));
       r_x1 = __ldg(reinterpret_cast<const float4*>(wt + 4));
       r_y = __ldg(wt + 8 + iy);
