@@ -162,6 +162,8 @@ struct nfft_plan {
   cudaStream_t zero_stream = nullptr;
   cudaEvent_t ev_grid2_used = nullptr, ev_grid2_zeroed = nullptr;
   bool skip_memset = false;
+  bool spread_zero_copy = true;    // table spreader: clear the tile by a bulk copy of zero_tile
+  void* zero_tile = nullptr;       // 128 KB of zeros
   bool fft_staged = true;          // FP32 line FFTs: tile staged by cp.async, in-place four-step
   bool spread_rec = true;          // 3-D FP32 table spreader: one-step staging with per-warp records
   int gather_pf = 4;               // TMA gather: L2 prefetch of the tile gather_pf x (SM count) tasks ahead (0: off)        // set while the spreading target is known to be zero

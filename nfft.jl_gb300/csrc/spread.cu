@@ -79,10 +79,23 @@ int tile3_rec_launch(nfft_plan* p, const Geom<float>& G, const Nodes<float>& Nd,
   using TR = Tile3Rec<BX, BY, BZ>;
   const CUtensorMap* map = (ncols == 1 && p->spread_tma) ? tile3_map<BX, BY, BZ>(p, gp) : nullptr;
   CUtensorMap none{};
+  // a zeroed buffer of the largest padded tile, copied into shared memory to
+  // clear each CTA's tile (allocated once per plan)
+  static_assert(TC::NACC * 8 <= 128 * 1024, "zero tile buffer");
+  if (!p->zero_tile && p->spread_zero_copy) {
+    if (cudaMalloc(&p->zero_tile, 128 * 1024) != cudaSuccess ||
+        cudaMemsetAsync(p->zero_tile, 0, 128 * 1024, p->stream) != cudaSuccess) {
+      cudaFree(p->zero_tile);
+      p->zero_tile = nullptr;
+      p->spread_zero_copy = false;  // plain stores clear the tile
+      cudaGetLastError();
+    }
+  }
   auto kr = spread_tile3_rec_kernel<BX, BY, BZ>;
   NFFT_CUDA_TRY(cudaFuncSetAttribute(kr, cudaFuncAttributeMaxDynamicSharedMemorySize, int(TR::SMEM)));
   kr<<<dim3(unsigned(p->n_tasks), unsigned(ncols)), TC::THREADS, TR::SMEM, p->stream>>>(
-      map ? *map : none, map ? 1 : 0, G, Nd, p->tasks, fhat, gp, ncols > 1 ? fcol : 0, gcol_t);
+      map ? *map : none, map ? 1 : 0, G, Nd, p->tasks, fhat, gp, ncols > 1 ? fcol : 0, gcol_t,
+      p->spread_zero_copy ? static_cast<const float4*>(p->zero_tile) : nullptr, p->dflag + 1);
   NFFT_LAUNCH_CHECK();
   return NFFT_OK;
 }

@@ -187,7 +187,9 @@ template <int BX, int BY, int BZ> struct Tile3Rec {
   using TC = Tile3<BX, BY, BZ>;
   static constexpr int NB = 32;
   static constexpr size_t REC_BYTES = size_t(NB) * 8 * 16;  // float4 [NB][8 warps]
-  static constexpr size_t SMEM = TC::ACC_BYTES + REC_BYTES + size_t(NB) * 64 * 4;
+  static constexpr size_t XY_OFF = TC::ACC_BYTES + REC_BYTES;
+  static constexpr size_t BAR_OFF = XY_OFF + size_t(NB) * 64 * 4;  // mbarrier of the tile's zero fill
+  static constexpr size_t SMEM = BAR_OFF + 16;
 };
 
 template <int BX, int BY, int BZ>
@@ -195,7 +197,8 @@ __global__ void __launch_bounds__(256, 4) spread_tile3_rec_kernel(const __grid_c
                                                                 Geom<float> G, Nodes<float> Nd,
                                                                 const int4* __restrict__ tasks,
                                                                 const float2* __restrict__ fhat,
-                                                                float* __restrict__ g, int64_t fcol, int64_t gcol) {
+                                                                float* __restrict__ g, int64_t fcol, int64_t gcol,
+                                                                const float4* __restrict__ zeros, int* status) {
   using TC = Tile3<BX, BY, BZ>;
   using TR = Tile3Rec<BX, BY, BZ>;
   constexpr int NB = TR::NB, PITCH = TC::PITCH, PLANE = TC::PLANE;
@@ -204,19 +207,35 @@ __global__ void __launch_bounds__(256, 4) spread_tile3_rec_kernel(const __grid_c
   g += blockIdx.y * gcol;
   float2* acc = reinterpret_cast<float2*>(smem_raw);
   float4* s_rec = reinterpret_cast<float4*>(smem_raw + TC::ACC_BYTES);        // [NB][8]
-  float* s_xy = reinterpret_cast<float*>(smem_raw + TC::ACC_BYTES + TR::REC_BYTES);  // [NB][64]
+  float* s_xy = reinterpret_cast<float*>(smem_raw + TR::XY_OFF);  // [NB][64]
+  const unsigned acc_s = static_cast<unsigned>(__cvta_generic_to_shared(acc));
+  const unsigned bar_s = static_cast<unsigned>(__cvta_generic_to_shared(smem_raw + TR::BAR_OFF));
   const int4 task = tasks[blockIdx.x];
   const int tile = task.x;
   const int tc0 = tile % G.ntiles[0];
   const int tc1 = (tile / G.ntiles[0]) % G.ntiles[1];
   const int tc2 = tile / (G.ntiles[0] * G.ntiles[1]);
   const int o0 = tc0 * BX, o1 = tc1 * BY, o2 = tc2 * BZ;
-  {
+  // zero fill of the tile: one bulk copy from a zeroed global buffer (the
+  // copy engine writes shared memory; the load/store pipe stays free for the
+  // staging), or plain stores without that buffer
+  if (zeros) {
+    if (threadIdx.x == 0) {
+      mbar_init(bar_s, 1);
+      asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+      mbar_expect_tx(bar_s, unsigned(TC::NACC) * 8u);
+      asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                       acc_s),
+                   "l"(zeros), "r"(unsigned(TC::NACC) * 8u), "r"(bar_s)
+                   : "memory");
+    }
+  } else {
     float4* a4 = reinterpret_cast<float4*>(acc);
     for (int q = threadIdx.x; q < TC::NACC / 2; q += TC::THREADS) a4[q] = make_float4(0.f, 0.f, 0.f, 0.f);
   }
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int s = threadIdx.x >> 3, iy = threadIdx.x & 7, hsel = (iy >> 2) & 1;
+  bool zeroed = zeros == nullptr;  // the zero fill has landed
 
   // register prefetch of this thread's node of one batch
   int4 r_nd = make_int4(0, 0, 0, 0);
@@ -259,6 +278,10 @@ __global__ void __launch_bounds__(256, 4) spread_tile3_rec_kernel(const __grid_c
     }
     __syncthreads();
     if (b + NB < task.z) prefetch(b + NB);
+    if (!zeroed) {  // (bounded: on timeout the CTA raises its status bit and adds nothing)
+      zeroed = __syncthreads_and(mbar_wait_bounded(bar_s, 0));  // the whole CTA agrees
+      if (!zeroed) break;
+    }
     // taps: warp w updates its slice of every node, rows iy and iy + 4 of the
     // lane's column; the next node's record is loaded during this node's taps
     float4 rt = s_rec[warp];
@@ -278,19 +301,23 @@ __global__ void __launch_bounds__(256, 4) spread_tile3_rec_kernel(const __grid_c
     }
     __syncthreads();
   }
+  // a task without nodes (or a timed-out wait) still waits for its zero
+  // fill, so that no copy into shared memory outlives the CTA
+  if (!zeroed) zeroed = mbar_wait_bounded(bar_s, 0);
   // the tile's shared-memory writes, made visible to the bulk (async) copy
   asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-  __syncthreads();
+  if (!__syncthreads_and(zeroed)) {
+    if (threadIdx.x == 0) atomicOr(status, 1);
+    return;
+  }
   const int q0 = wrap_once(o0 + G.sh[0], G.Nt[0]), q1 = wrap_once(o1 + G.sh[1], G.Nt[1]);
   const int q2 = wrap_once(o2 + G.sh[2], G.Nt[2]);
-  if (use_tma && tile3_interior<BX, BY, BZ>(G, q0, q1, q2) &&
-      (static_cast<unsigned>(__cvta_generic_to_shared(acc)) & 127u) == 0) {
+  if (use_tma && tile3_interior<BX, BY, BZ>(G, q0, q1, q2) && (acc_s & 127u) == 0) {
     if (threadIdx.x == 0) {
       const int x = 2 * (q0 - 4), y = q1 - 3, z = q2 - 3;  // x in floats: a multiple of 4 (16 bytes)
-      const unsigned src = static_cast<unsigned>(__cvta_generic_to_shared(acc));
       asm volatile(
           "cp.reduce.async.bulk.tensor.3d.global.shared::cta.add.tile.bulk_group [%0, {%1, %2, %3}], [%4];"
-          ::"l"(reinterpret_cast<uint64_t>(&tmap)), "r"(x), "r"(y), "r"(z), "r"(src)
+          ::"l"(reinterpret_cast<uint64_t>(&tmap)), "r"(x), "r"(y), "r"(z), "r"(acc_s)
           : "memory");
       asm volatile("cp.async.bulk.commit_group;" ::: "memory");
       asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");  // the tile has been read before exit

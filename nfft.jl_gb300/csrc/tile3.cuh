@@ -52,6 +52,12 @@ __device__ __forceinline__ bool mbar_try_wait(unsigned addr, unsigned parity) {
       : "memory");
   return ok != 0;
 }
+// Bounded wait for the phase with the given parity: false after 2^22 polls.
+__device__ __forceinline__ bool mbar_wait_bounded(unsigned addr, unsigned parity) {
+  for (int it = 0; it < (1 << 22); ++it)
+    if (mbar_try_wait(addr, parity)) return true;
+  return false;
+}
 
 // The grid region of a tile's padded box lies inside the grid (no wrap):
 // the box is added with one bulk tensor reduction.

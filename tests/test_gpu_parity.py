@@ -325,18 +325,22 @@ def test_paper_accuracy_d2_tensor_gpu_fp64():
 
 @pytest.mark.parametrize("bs", [(16, 8, 8), (16, 16, 8), (32, 8, 8), (8, 8, 8)])
 @pytest.mark.parametrize("pre", [oracle.TENSOR, oracle.POLYNOMIAL])
-@pytest.mark.parametrize("path", ["tma", "points", "generic", "tma-two-step", "points-two-step"])
+@pytest.mark.parametrize("path", ["tma", "points", "generic", "tma-two-step", "points-two-step", "tma-zero-stores"])
 def test_specialised_3d_spreader(monkeypatch, bs, pre, path):
     """The shape-specialised 3-D FP32 m = 4 spreader, with the bulk tensor
     reduction flush for tiles inside the grid ("tma"), with the per-point
     flush only ("points"), and the generic kernel ("generic"), all give the
     oracle's adjoint; table windows run the one-step staging with per-warp
     records by default and the two-step staging with
-    NFFT_GB300_SPREAD_REC=0 ("-two-step").  The grid has interior tiles and
-    tiles that wrap in every dimension, boundary nodes included."""
+    NFFT_GB300_SPREAD_REC=0 ("-two-step"); the one-step kernel clears its
+    tile by a bulk copy of zeros by default and by plain stores with
+    NFFT_GB300_SPREAD_ZERO_COPY=0 ("-zero-stores").  The grid has interior
+    tiles and tiles that wrap in every dimension, boundary nodes included, and
+    the plan's status stays clean."""
     monkeypatch.setenv("NFFT_GB300_SPREAD_TILE3", "0" if path == "generic" else "1")
     monkeypatch.setenv("NFFT_GB300_SPREAD_TMA", "1" if path.startswith("tma") else "0")
     monkeypatch.setenv("NFFT_GB300_SPREAD_REC", "0" if path.endswith("two-step") else "1")
+    monkeypatch.setenv("NFFT_GB300_SPREAD_ZERO_COPY", "0" if path.endswith("zero-stores") else "1")
     N = (48, 40, 36)
     k, f, fhat = rand_problem(3, N, 30000, seed=300, dtype=np.float32)
     k[:, :5] = np.array([[-0.5, 0.4999, 0.0, -0.001, 0.25]] * 3, dtype=np.float32)
@@ -349,6 +353,7 @@ def test_specialised_3d_spreader(monkeypatch, bs, pre, path):
     p.convolve_transpose_(torch.as_tensor(fhat).to(p.cdtype).cuda(), g)
     ref = op.convolve_transpose(fhat.astype(np.complex128))
     assert oracle.rel_l2(colmajor_flat(g.cpu().numpy()), colmajor_flat(ref)) < TOL32
+    assert nf.load().nfft_sync(p._handle) == 0
 
 
 @pytest.mark.parametrize("bs", [(16, 8, 8), (16, 16, 8), (32, 8, 8), (8, 8, 8)])
