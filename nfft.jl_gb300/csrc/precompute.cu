@@ -137,21 +137,38 @@ __global__ void deconv_factors_kernel(int window, int m, double sigma, int D, in
 
 // ------------------------------------------------------- spreading tasks
 // One task per chunk of at most `chunk` nodes of a non-empty home tile.
-__global__ void task_counts_kernel(const int32_t* __restrict__ tstart, int64_t ntiles, int chunk,
+// Tasks are listed in raster order of the tiles shifted by half the grid in
+// every dimension: list position q holds tile ((q_d + nt_d / 2) mod nt_d)_d.
+// The tiles at the grid's corners (the centre of k-space, where the nodes are
+// dense and the tasks long) then sit in the middle of the launch, and the
+// last CTAs of a launch take the short tasks of the grid's middle, so no SM
+// is left with a long task while the others idle.
+struct TileOrder {
+  int n0, n1, n2;
+  __device__ __forceinline__ int tile(int64_t q) const {
+    const int q0 = int(q % n0), q1 = int((q / n0) % n1), q2 = int(q / (int64_t(n0) * n1));
+    const int t0 = (q0 + n0 / 2) % n0, t1 = (q1 + n1 / 2) % n1, t2 = (q2 + n2 / 2) % n2;
+    return t0 + n0 * (t1 + n1 * t2);
+  }
+};
+
+__global__ void task_counts_kernel(const int32_t* __restrict__ tstart, int64_t ntiles, int chunk, TileOrder order,
                                    int32_t* __restrict__ tcnt) {
-  int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (t >= ntiles) return;
+  int64_t q = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (q >= ntiles) return;
+  const int t = order.tile(q);
   const int n = tstart[t + 1] - tstart[t];
-  tcnt[t] = (n + chunk - 1) / chunk;
+  tcnt[q] = (n + chunk - 1) / chunk;
 }
 
 __global__ void fill_tasks_kernel(const int32_t* __restrict__ tstart, const int32_t* __restrict__ toff,
-                                  int64_t ntiles, int chunk, int4* __restrict__ tasks) {
-  int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (t >= ntiles) return;
+                                  int64_t ntiles, int chunk, TileOrder order, int4* __restrict__ tasks) {
+  int64_t q = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (q >= ntiles) return;
+  const int t = order.tile(q);
   const int s = tstart[t], e = tstart[t + 1];
-  int pos = toff[t];
-  for (int b = s; b < e; b += chunk) tasks[pos++] = make_int4(int(t), b, min(e, b + chunk), 0);
+  int pos = toff[q];
+  for (int b = s; b < e; b += chunk) tasks[pos++] = make_int4(t, b, min(e, b + chunk), 0);
 }
 
 }  // namespace
@@ -247,7 +264,8 @@ int launch_build_tasks(nfft_plan* p, int chunk) {
   auto* toff = static_cast<int32_t*>(node_buffer(p, nfft_plan::NB_TOFF, sizeof(int32_t) * (nt + 1)));
   void* scr = node_buffer(p, nfft_plan::NB_SCR, std::max(sb, p->nbuf_cap[nfft_plan::NB_SCR]));
   if (!tcnt || !toff || !scr) return NFFT_ERR_ALLOC;
-  task_counts_kernel<<<unsigned((nt + 255) / 256), 256, 0, p->stream>>>(p->tile_start, nt, chunk, tcnt);
+  const TileOrder order{int(p->ntiles[0]), int(p->ntiles[1]), int(p->ntiles[2])};
+  task_counts_kernel<<<unsigned((nt + 255) / 256), 256, 0, p->stream>>>(p->tile_start, nt, chunk, order, tcnt);
   NFFT_LAUNCH_CHECK();
   NFFT_CUDA_TRY(cudaMemsetAsync(tcnt + nt, 0, sizeof(int32_t), p->stream));
   int rc = exclusive_scan_i32(tcnt, toff, nt + 1, scr, p->nbuf_cap[nfft_plan::NB_SCR], p->stream);
@@ -259,7 +277,8 @@ int launch_build_tasks(nfft_plan* p, int chunk) {
   p->tasks = static_cast<int4*>(node_buffer(p, nfft_plan::NB_TASKS, sizeof(int4) * size_t(ntasks)));
   if (!p->tasks) return NFFT_ERR_ALLOC;
   if (ntasks > 0) {
-    fill_tasks_kernel<<<unsigned((nt + 255) / 256), 256, 0, p->stream>>>(p->tile_start, toff, nt, chunk, p->tasks);
+    fill_tasks_kernel<<<unsigned((nt + 255) / 256), 256, 0, p->stream>>>(p->tile_start, toff, nt, chunk, order,
+                                                                          p->tasks);
     NFFT_LAUNCH_CHECK();
   }
   return NFFT_OK;
