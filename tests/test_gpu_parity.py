@@ -185,6 +185,9 @@ FUSED_CASES = [
     ((51, 26), 2.5),           # odd N: head 26 / tail 25 image rows; Ntilde (128, 64)
     ((32, 64, 32), 2.0),
     ((26, 51, 26), 2.5),       # Ntilde (64, 128, 64)
+    ((128, 32, 32), 2.0),      # Ntilde (256, 64, 64)
+    ((256, 32, 32), 2.0),      # Ntilde (512, 64, 64): the headline's x-line kernels
+    ((205, 26, 26), 2.5),      # Ntilde (512, 64, 64), odd N0
 ]
 
 
