@@ -52,17 +52,18 @@ def config_dict(**kw):
     return cfg
 # DRAM bytes (read + write) per launch of the dominant kernel on this workload,
 # from one ncu capture (dram__bytes_read.sum + dram__bytes_write.sum, one
-# launch, tiles 16x8x8): 1.17 GB read + 0.602 GB write.  Not measured in the
+# launch, tiles 16x8x8): 1.157 GB read + 0.578 GB write.  Not measured in the
 # run itself; the line says so.
-SPREAD_DRAM_BYTES = 1.774e9
-SPREAD_TRAFFIC_SOURCE = "ncu capture of spread_tile3_kernel on this workload (one launch), not measured in this run"
+SPREAD_DRAM_BYTES = 1.735e9
+SPREAD_TRAFFIC_SOURCE = ("ncu capture of spread_tile3_rec_kernel on this workload (one launch), "
+                         "not measured in this run")
 # DRAM bytes (read + write) of one Toeplitz application at 256^3 (the five
 # kernels of the fused path), from an ncu capture of the profiling case:
 # 2.821 GB read + 1.049 GB write.
 TOEPLITZ_DRAM_BYTES = 3.870e9
-SPREAD_LIMITER = ("shared-memory wavefronts ~65% and instruction issue ~60% of peak (ncu, 128^3 case): the "
-                  "read-modify-write of the padded tile in shared memory (16 B per tap; 512 taps per node) "
-                  "bounds the kernel, HBM is not the limiter (DRAM throughput ~6%)")
+SPREAD_LIMITER = ("shared-memory wavefronts: 110 per node (ncu, 128^3 case; 4.6e8 per launch = 1.47 ms at one "
+                  "per clock per SM, ~91% of it reached) -- the read-modify-write of the padded tile in shared "
+                  "memory (16 B per tap; 512 taps per node) bounds the kernel; HBM is not the limiter")
 
 
 def radial_nodes(dtype=np.float32):
@@ -487,7 +488,8 @@ def run_ours(args):
     dom = max(alg, key=lambda s: stages[s])
     t_dom = stages[dom] * 1e-3
     achieved = alg[dom] / t_dom / 1e9
-    kernel_names = {"spread_ms": "spread_tile3_kernel (stage: value sort + kernel; its grid was zeroed on a side stream beside the previous gather)",
+    kernel_names = {"spread_ms": "spread_tile3_rec_kernel (stage: the kernel alone; its grid was zeroed on a side "
+                                 "stream beside the previous gather)",
                     "gather_ms": "interp_tile3_kernel", "deconv_pad_ms": "fft4_x_kernel (forward)",
                     "crop_ms": "fft4_x_kernel (adjoint)"}
     roofline = {"bound": "hbm", "kernel": kernel_names[dom], "achieved": achieved, "peak": peak, "unit": "GB/s",
