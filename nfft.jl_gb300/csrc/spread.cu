@@ -91,20 +91,24 @@ int tile3_rec_launch(nfft_plan* p, const Geom<float>& G, const Nodes<float>& Nd,
       cudaGetLastError();
     }
   }
-  auto kr = spread_tile3_rec_kernel<BX, BY, BZ>;
+  WinCoeffs8 wc{};
+  if (!p->wtab)
+    for (int q = 0; q < 8 * 9; ++q) wc.c[q] = float(p->coeffs_host[q]);
+  auto kr = p->wtab ? spread_tile3_rec_kernel<BX, BY, BZ, true> : spread_tile3_rec_kernel<BX, BY, BZ, false>;
   NFFT_CUDA_TRY(cudaFuncSetAttribute(kr, cudaFuncAttributeMaxDynamicSharedMemorySize, int(TR::SMEM)));
   kr<<<dim3(unsigned(p->n_tasks), unsigned(ncols)), TC::THREADS, TR::SMEM, p->stream>>>(
       map ? *map : none, map ? 1 : 0, G, Nd, p->tasks, fhat, gp, ncols > 1 ? fcol : 0, gcol_t,
-      p->spread_zero_copy ? static_cast<const float4*>(p->zero_tile) : nullptr, p->dflag + 1);
+      p->spread_zero_copy ? static_cast<const float4*>(p->zero_tile) : nullptr, p->dflag + 1, wc);
   NFFT_LAUNCH_CHECK();
   return NFFT_OK;
 }
 
-// The one-step kernel when the plan's tiles have a shape-specialised form and
-// its window values come from the table (no value sort); -1 = not applicable.
+// The one-step kernel when the plan's tiles have a shape-specialised form
+// (no value sort); -1 = not applicable.
 int spread_tile3_user(nfft_plan* p, const Geom<float>& G, const Nodes<float>& Nd, const float2* fhat, float* gp,
                       int ncols, int64_t fcol, int64_t gcol_t) {
-  if (!p->spread_tile3 || !p->spread_rec || !p->wtab || p->D != 3 || p->m != 4 || p->prm.compensated ||
+  if (!p->spread_tile3 || !p->spread_rec || (!p->wtab && !p->frac4) || p->D != 3 || p->m != 4 ||
+      p->prm.compensated ||
       p->spread_layout != 1 || p->bs[2] != 8)
     return -1;
   const int64_t bx = p->bs[0], by = p->bs[1];

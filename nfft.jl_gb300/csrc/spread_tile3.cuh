@@ -173,12 +173,13 @@ __global__ void __launch_bounds__(256) spread_tile3_kernel(const __grid_constant
   flush_tile<3, float, false, 8>(G, acc + 1, g, o0, o1, o2, TC::P0 - 1, TC::P1, TC::P2, PITCH);
 }
 
-// Variant for window values from the table with one staging step: thread
-// (node s, row iy) of a batch loads the node's record, value (from the
-// caller's order through the node's input index: no separate value sort)
-// and window values itself (a batch ahead, in registers) and writes row iy of the x-y
-// products and the 16-byte record of owner warp iy: {offset of the warp's
-// first tap in the padded tile, value x z window value of its slice}.  The
+// Variant with one staging step: thread (node s, row iy) of a batch loads
+// the node's record, value (from the caller's order through the node's input
+// index: no separate value sort) and window values (from the table, or its
+// fractional offsets for Horner evaluation) itself, a batch ahead in
+// registers, and writes row iy of the x-y products and the 16-byte record of
+// the warp that owns window slice iy, warp (z0 + iy) mod 8: {offset of the
+// warp's first tap in the padded tile, value x z window value iy}.  The
 // tap loop then reads one broadcast record per node instead of a node record
 // and a slice value, and the staging needs neither a window-value area nor a
 // second CTA barrier: ~11 instead of ~15 shared-memory wavefronts per node
@@ -192,13 +193,28 @@ template <int BX, int BY, int BZ> struct Tile3Rec {
   static constexpr size_t SMEM = BAR_OFF + 16;
 };
 
-template <int BX, int BY, int BZ>
+// The polynomial window's coefficients, column l at c[9 l .. 9 l + 8]
+// (degree 2m = 8 at m = 4), passed by value so that uniform reads hit the
+// constant cache.
+struct WinCoeffs8 {
+  float c[8 * 9];
+};
+
+__device__ __forceinline__ float horner9(const float* c, float t) {
+  float v = c[8];
+#pragma unroll
+  for (int i = 7; i >= 0; --i) v = fmaf(v, t, c[i]);
+  return v;
+}
+
+template <int BX, int BY, int BZ, bool TABLE>
 __global__ void __launch_bounds__(256, 4) spread_tile3_rec_kernel(const __grid_constant__ CUtensorMap tmap, int use_tma,
                                                                 Geom<float> G, Nodes<float> Nd,
                                                                 const int4* __restrict__ tasks,
                                                                 const float2* __restrict__ fhat,
                                                                 float* __restrict__ g, int64_t fcol, int64_t gcol,
-                                                                const float4* __restrict__ zeros, int* status) {
+                                                                const float4* __restrict__ zeros, int* status,
+                                                                const __grid_constant__ WinCoeffs8 wc) {
   using TC = Tile3<BX, BY, BZ>;
   using TR = Tile3Rec<BX, BY, BZ>;
   constexpr int NB = TR::NB, PITCH = TC::PITCH, PLANE = TC::PLANE;
@@ -237,22 +253,32 @@ __global__ void __launch_bounds__(256, 4) spread_tile3_rec_kernel(const __grid_c
   const int s = threadIdx.x >> 3, iy = threadIdx.x & 7, hsel = (iy >> 2) & 1;
   bool zeroed = zeros == nullptr;  // the zero fill has landed
 
-  // register prefetch of this thread's node of one batch
+  // register prefetch of this thread's node of one batch: record, value,
+  // and the x window values with y / z window value iy (table) or the
+  // fractional offsets (Horner)
   int4 r_nd = make_int4(0, 0, 0, 0);
   float2 r_c = make_float2(0.f, 0.f);
-  float4 r_x0 = make_float4(0.f, 0.f, 0.f, 0.f), r_x1 = r_x0, r_z0 = r_x0, r_z1 = r_x0;
-  float r_y = 0.f;
+  float4 r_x0 = make_float4(0.f, 0.f, 0.f, 0.f), r_x1 = r_x0, r_f = r_x0;
+  float r_y = 0.f, r_z = 0.f;
+  float cy[9];  // Horner: the coefficients of window column iy
+  if constexpr (!TABLE) {
+#pragma unroll
+    for (int i = 0; i < 9; ++i) cy[i] = wc.c[iy * 9 + i];
+  }
   auto prefetch = [&](int b) {
     const int j = b + s;
     if (j < task.z) {
-      const float* wt = Nd.wtab + int64_t(j) * 24;
       r_nd = __ldg(Nd.node4 + j);
       r_c = __ldg(fhat + r_nd.w);
-      r_x0 = __ldg(reinterpret_cast<const float4*>(wt));
-      r_x1 = __ldg(reinterpret_cast<const float4*>(wt + 4));
-      r_y = __ldg(wt + 8 + iy);
-      r_z0 = __ldg(reinterpret_cast<const float4*>(wt + 16));
-      r_z1 = __ldg(reinterpret_cast<const float4*>(wt + 20));
+      if constexpr (TABLE) {
+        const float* wt = Nd.wtab + int64_t(j) * 24;
+        r_x0 = __ldg(reinterpret_cast<const float4*>(wt));
+        r_x1 = __ldg(reinterpret_cast<const float4*>(wt + 4));
+        r_y = __ldg(wt + 8 + iy);
+        r_z = __ldg(wt + 16 + iy);
+      } else {
+        r_f = __ldg(reinterpret_cast<const float4*>(Nd.frac4) + j);
+      }
     }
   };
   if (task.y < task.z) prefetch(task.y);
@@ -262,19 +288,26 @@ __global__ void __launch_bounds__(256, 4) spread_tile3_rec_kernel(const __grid_c
   for (int b = task.y; b < task.z; b += NB) {
     const int n = min(NB, task.z - b);
     if (s < n) {
-      // the record of owner warp iy: its slice is = (iy - z0) mod 8 of the window
+      float wy = r_y, wz = r_z;
+      if constexpr (!TABLE) {  // evalpoly(frac - 1/2, coefficients of column l)
+        const float tx = r_f.x - 0.5f;
+        r_x0 = make_float4(horner9(wc.c + 0, tx), horner9(wc.c + 9, tx), horner9(wc.c + 18, tx),
+                           horner9(wc.c + 27, tx));
+        r_x1 = make_float4(horner9(wc.c + 36, tx), horner9(wc.c + 45, tx), horner9(wc.c + 54, tx),
+                           horner9(wc.c + 63, tx));
+        wy = horner9(cy, r_f.y - 0.5f);
+        wz = horner9(cy, r_f.z - 0.5f);
+      }
+      // the record of the warp that owns window slice iy (tile plane z0 + iy)
       const int z0 = r_nd.z - o2;
-      const int is = (iy - z0) & 7;
-      const float wz = is < 4 ? (is < 2 ? (is == 0 ? r_z0.x : r_z0.y) : (is == 2 ? r_z0.z : r_z0.w))
-                              : (is < 6 ? (is == 4 ? r_z1.x : r_z1.y) : (is == 6 ? r_z1.z : r_z1.w));
-      const int off = (z0 + is) * PLANE + (r_nd.y - o1) * PITCH + (r_nd.x - o0 + 1);
-      s_rec[s * 8 + iy] = make_float4(__int_as_float(off), 0.f, r_c.x * wz, r_c.y * wz);
+      const int off = (z0 + iy) * PLANE + (r_nd.y - o1) * PITCH + (r_nd.x - o0 + 1);
+      s_rec[s * 8 + ((z0 + iy) & 7)] = make_float4(__int_as_float(off), 0.f, r_c.x * wz, r_c.y * wz);
       // row iy of the x-y products; the two halves in an order that keeps
       // the eight lanes of each 128-bit store phase on distinct banks
       float4* out = reinterpret_cast<float4*>(s_xy + s * 64 + iy * 8);
       const float4 xa = hsel ? r_x1 : r_x0, xb = hsel ? r_x0 : r_x1;
-      out[hsel] = make_float4(xa.x * r_y, xa.y * r_y, xa.z * r_y, xa.w * r_y);
-      out[hsel ^ 1] = make_float4(xb.x * r_y, xb.y * r_y, xb.z * r_y, xb.w * r_y);
+      out[hsel] = make_float4(xa.x * wy, xa.y * wy, xa.z * wy, xa.w * wy);
+      out[hsel ^ 1] = make_float4(xb.x * wy, xb.y * wy, xb.z * wy, xb.w * wy);
     }
     __syncthreads();
     if (b + NB < task.z) prefetch(b + NB);
