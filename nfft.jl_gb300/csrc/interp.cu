@@ -270,13 +270,15 @@ __global__ void __launch_bounds__(kInterpThreads) interp_tile_kernel(Geom<T> G, 
 template <bool TABLE> struct Tile3Gather {
   static constexpr int NK = 4;
   static constexpr int WCH = TABLE ? 6 : 1;
-  static constexpr int SLOT = NK * (16 + 16 * WCH);
+  // records, window values (copied from the table, or evaluated by Horner
+  // from the fractional offsets staged behind them)
+  static constexpr int SLOT = NK * (16 + 96 + (TABLE ? 0 : 16));
   static constexpr int NS = 2;  // (3 slots measured the same, 4 cost a CTA per SM)
   static constexpr size_t STAGE_BYTES = size_t(kInterpThreads / 32) * NS * SLOT;
 };
 
 template <int BX, int BY, int BZ, bool TABLE>
-__global__ void __launch_bounds__(kInterpThreads) interp_tile3_kernel(const __grid_constant__ CUtensorMap tmap,
+__global__ void __launch_bounds__(kInterpThreads, 4) interp_tile3_kernel(const __grid_constant__ CUtensorMap tmap,
                                                                        Geom<float> G, Nodes<float> Nd,
                                                                        const int4* __restrict__ tasks,
                                                                        const float2* __restrict__ g,
@@ -324,7 +326,7 @@ __global__ void __launch_bounds__(kInterpThreads) interp_tile3_kernel(const __gr
   // within a task fit in 32 bits
   const bool win_lane = lane < NK * WCH, rec_lane = lane >= 24 && lane < 24 + NK;
   const int cp_k = win_lane ? lane / WCH : lane - 24, cp_c = win_lane ? lane % WCH : 0;
-  const int cp_dst = win_lane ? NK * 16 + cp_k * 16 * WCH + 16 * cp_c : 16 * cp_k;
+  const int cp_dst = win_lane ? (TABLE ? NK * 16 + cp_k * 96 + 16 * cp_c : NK * (16 + 96) + 16 * cp_k) : 16 * cp_k;
   auto stage = [&](int buf, int gbase) {
     const int id = gbase + cp_k;
     if ((win_lane || rec_lane) && id < task.z) {
@@ -378,7 +380,20 @@ __global__ void __launch_bounds__(kInterpThreads) interp_tile3_kernel(const __gr
     stage(buf == 0 ? NS - 1 : buf - 1, base + (NS - 1) * NK * NWARPS);
     asm volatile("cp.async.wait_group %0;" ::"n"(NS - 1) : "memory");  // this group's slot has landed
     __syncwarp();
-    const unsigned char* st = stage_base + buf * SLOT;
+    unsigned char* st = stage_base + buf * SLOT;
+    if constexpr (!TABLE) {
+      // the group's 4 x 24 window values, three per lane: value q = lane + 32 r
+      // is column q mod 8 = lane mod 8 (the lane's coefficients) of dimension
+      // (q mod 24) / 8 of node q / 24, evalpoly(frac - 1/2, coefficients)
+      const float* fr = reinterpret_cast<const float*>(st + NK * (16 + 96));
+      float* wv = reinterpret_cast<float*>(st + NK * 16);
+#pragma unroll
+      for (int r = 0; r < 3; ++r) {
+        const int q = lane + 32 * r, k = q / 24, d = (q % 24) / 8;
+        if (base + k < task.z) wv[q] = P.eval(0, fr[4 * k + d]);
+      }
+      __syncwarp();
+    }
     const int4* rec = reinterpret_cast<const int4*>(st);
     const float* win = reinterpret_cast<const float*>(st + NK * 16);
     float ar[NK], ai[NK];
@@ -387,7 +402,7 @@ __global__ void __launch_bounds__(kInterpThreads) interp_tile3_kernel(const __gr
       const int4 nd = rec[k];
       // window values: x at the lane's column, y at its two rows, all 8 z
       float wx, wy0, wy1, wz[8];
-      if constexpr (TABLE) {  // broadcast reads of the staged table values
+      {  // broadcast reads of the staged window values
         const float* wt = win + k * 24;
         wx = wt[ix];
         wy0 = wt[8 + ry];
@@ -396,14 +411,6 @@ __global__ void __launch_bounds__(kInterpThreads) interp_tile3_kernel(const __gr
         const float4 z1 = *reinterpret_cast<const float4*>(wt + 20);
         wz[0] = z0.x, wz[1] = z0.y, wz[2] = z0.z, wz[3] = z0.w;
         wz[4] = z1.x, wz[5] = z1.y, wz[6] = z1.z, wz[7] = z1.w;
-      } else {  // one value per lane by Horner, then shuffled
-        float W[LN::NW];
-        W[0] = lane < 24 ? P.eval(0, win[k * 4 + lane / 8]) : 0.f;
-        wx = wsel<3, 8>(W, ix);
-        wy0 = wsel<3, 8>(W, 8 + ry);
-        wy1 = wsel<3, 8>(W, 12 + ry);
-#pragma unroll
-        for (int iz = 0; iz < 8; ++iz) wz[iz] = wsel<3, 8>(W, 16 + iz);
       }
       // (a node past the task end reads tap 0 of the tile and is dropped)
       const float2* bp = tile + (valid ? nd.z * PLANE + nd.y * PITCH + nd.x + lane_off : 0);
