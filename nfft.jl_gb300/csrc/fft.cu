@@ -616,6 +616,30 @@ __global__ void __launch_bounds__(256, FWD ? 3 : 2) fft4_lines_kernel(LineGeom L
   }
 }
 
+// Marks, for every block of kW4 x columns and every y of the (centred)
+// grid, the 8-position z groups that the padded tile of some bin with nodes
+// covers: bin tile t spans x [o0 - m - 1, o0 + bx + m), y and z
+// [o - m, o + b + m) around its origin o (+ the grid shift sh, modulo Ntilde).
+__global__ void zmask_kernel(const int32_t* __restrict__ tstart, int nt0, int nt1, int nt2, int bx, int by, int bz,
+                             int m, int Nt0, int Nt1, int Nt2, int sh0, int sh1, int sh2, int tiles_x,
+                             unsigned long long* __restrict__ zmask) {
+  const int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (t >= int64_t(nt0) * nt1 * nt2 || tstart[t + 1] == tstart[t]) return;
+  const int tx = int(t % nt0), ty = int((t / nt0) % nt1), tz = int(t / (int64_t(nt0) * nt1));
+  const int ox = tx * bx + sh0, oy = ty * by + sh1, oz = tz * bz + sh2;
+  unsigned long long bits = 0;
+  for (int z = oz - m; z < oz + bz + m; ++z) bits |= 1ull << (wrap_any(z, Nt2) >> 3);
+  const int x0 = ox - m - 1, x1 = ox + bx + m - 1;
+  for (int y = oy - m; y < oy + by + m; ++y) {
+    unsigned long long* row = zmask + int64_t(wrap_any(y, Nt1)) * tiles_x;
+    for (int x = x0;; x += kW4) {
+      const int xc = x < x1 ? x : x1;
+      atomicOr(row + wrap_any(xc, Nt0) / kW4, bits);
+      if (xc == x1) break;
+    }
+  }
+}
+
 // The same four-step line FFT with the CTA's W x NL tile staged in shared
 // memory first: every thread issues its share of 16-byte cp.async copies of
 // the tile at once (the forward copies only the image rows), so a CTA has
@@ -626,9 +650,17 @@ __global__ void __launch_bounds__(256, FWD ? 3 : 2) fft4_lines_kernel(LineGeom L
 // R2 k1 .. R2 k1 + R2 - 1; half-warps cover the 16 columns of one row in every
 // access, so no access has a bank conflict.  W x NL x 8 bytes of shared
 // memory (64 KB at NL = 512).
-template <int NL, bool FWD>
+//
+// zmask (z lines only, or null): bit b of zmask[y * tiles_x + x tile] says
+// whether grid positions z in [8 b, 8 b + 8) of those lines lie in the
+// padded tile of some bin with nodes.  The forward writes only those
+// positions (the gather reads nothing else; a line block with no such
+// position is skipped), the inverse reads only those (the spreading wrote
+// nothing else into the zeroed grid).
+template <int NL, bool FWD, bool MASKED>
 __global__ void __launch_bounds__(256, 3) fft4_lines_staged_kernel(LineGeom L, float2* __restrict__ g,
-                                                                   const float2* __restrict__ tw) {
+                                                                   const float2* __restrict__ tw,
+                                                                   const unsigned long long* __restrict__ zmask) {
   using C = float2;
   constexpr int R1 = Split4<NL>::R1, R2 = Split4<NL>::R2, W = kW4, S = FWD ? -1 : 1;
   static_assert(W == 16, "a row of the tile is 8 16-byte chunks");
@@ -639,10 +671,25 @@ __global__ void __launch_bounds__(256, 3) fft4_lines_staged_kernel(LineGeom L, f
   const int go = L.outer_N > 0 ? wrap_once(o - L.outer_N / 2, L.outer_Nt) : o;
   C* base = g + int64_t(go) * L.outer_stride + int64_t(tile) * W;
   const int head = L.n_img - L.n_img / 2, tail0 = NL - L.n_img / 2;
+  const unsigned long long live = MASKED ? __ldg(zmask + int64_t(o) * L.tiles_x + tile) : ~0ull;
+  if (MASKED && live == 0) {
+    // forward: no position of these lines is read; inverse: the lines are
+    // zero, and so are their transforms at the image positions
+    if (!FWD) {
+      const int nimg = head + (NL - tail0);
+      for (int c = threadIdx.x; c < nimg * 8; c += 256) {
+        const int r = c >> 3, part = c & 7;
+        const int pos = r < head ? r : tail0 + (r - head);
+        *reinterpret_cast<float4*>(base + int64_t(pos) * L.stride + 2 * part) = make_float4(0.f, 0.f, 0.f, 0.f);
+      }
+    }
+    return;
+  }
+  auto used = [&](int pos) { return !MASKED || ((live >> (pos >> 3)) & 1ull) != 0; };
   // stage the tile: NL rows of W complex values (8 chunks of 16 bytes)
   for (int c = threadIdx.x; c < NL * 8; c += 256) {
     const int row = c >> 3, part = c & 7;
-    if (!FWD || row < head || row >= tail0) {
+    if ((!FWD || row < head || row >= tail0) && (FWD || used(row))) {
       const unsigned dst = static_cast<unsigned>(__cvta_generic_to_shared(buf + row * W + 2 * part));
       asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst),
                    "l"(base + int64_t(row) * L.stride + 2 * part)
@@ -664,7 +711,7 @@ __global__ void __launch_bounds__(256, 3) fft4_lines_staged_kernel(LineGeom L, f
         const int n = R2 * n1 + n2;
         v[n1].x = 0.f;
         v[n1].y = 0.f;
-        if (!FWD || n < head || n >= tail0) v[n1] = buf[n * W + w];
+        if ((!FWD || n < head || n >= tail0) && (FWD || used(n))) v[n1] = buf[n * W + w];
       }
       dft_reg<S, R1>(v);
       twiddle4<S, NL, R1>(v, n2, tw);
@@ -687,7 +734,7 @@ __global__ void __launch_bounds__(256, 3) fft4_lines_staged_kernel(LineGeom L, f
 #pragma unroll
       for (int k2 = 0; k2 < R2; ++k2) {
         const int pos = k1 + R1 * k2;
-        if (FWD || pos < head || pos >= tail0) base[w + int64_t(pos) * L.stride] = v[k2];
+        if ((FWD && used(pos)) || (!FWD && (pos < head || pos >= tail0))) base[w + int64_t(pos) * L.stride] = v[k2];
       }
     }
   }
@@ -976,6 +1023,41 @@ LineGeom make_line_geom(const nfft_plan* p, int axis, int W, int64_t* outer_coun
   return L;
 }
 
+// The plan's z-line mask (see fft4_lines_staged_kernel), rebuilt when the
+// nodes, the tile shape or the grid shift changed; null when it does not
+// apply (not a 3-D FP32 binned plan on the staged path, z longer than 512,
+// NFFT_GB300_FFT_PRUNE=0, or a transform outside the centred scope).
+static const unsigned long long* zmask_for(nfft_plan* p) {
+  if (!p->fft_prune || p->D != 3 || p->precision != 32 || !p->prm.blocking || !p->tile_start || !p->has_nodes)
+    return nullptr;
+  if (p->Nt[2] > 512 || p->Nt[2] % 8 != 0 || p->Nt[0] % kW4 != 0) return nullptr;
+  int sh[3];
+  for (int d = 0; d < 3; ++d) sh[d] = p->cur_center ? int(p->sh[d]) : 0;
+  const int64_t key = (((p->nodes_version * 1024 + p->bs[0]) * 1024 + p->bs[1]) * 1024 + p->bs[2]) * 8 +
+                      (sh[0] != 0) * 4 + (sh[1] != 0) * 2 + (sh[2] != 0);
+  if (p->zmask && p->zmask_key == key) return static_cast<const unsigned long long*>(p->zmask);
+  const int tiles_x = int(p->Nt[0] / kW4);
+  const size_t bytes = sizeof(unsigned long long) * size_t(tiles_x) * size_t(p->Nt[1]);
+  if (!p->zmask && cudaMalloc(&p->zmask, bytes) != cudaSuccess) {
+    p->zmask = nullptr;
+    p->fft_prune = false;
+    cudaGetLastError();
+    return nullptr;
+  }
+  if (cudaMemsetAsync(p->zmask, 0, bytes, p->stream) != cudaSuccess) return nullptr;
+  const int64_t nt = p->ntiles_total;
+  if (nt > 0) {
+    ::nfft::g_launches.fetch_add(1, std::memory_order_relaxed);
+    zmask_kernel<<<unsigned((nt + 255) / 256), 256, 0, p->stream>>>(
+        p->tile_start, int(p->ntiles[0]), int(p->ntiles[1]), int(p->ntiles[2]), int(p->bs[0]), int(p->bs[1]),
+        int(p->bs[2]), p->m, int(p->Nt[0]), int(p->Nt[1]), int(p->Nt[2]), sh[0], sh[1], sh[2], tiles_x,
+        static_cast<unsigned long long*>(p->zmask));
+  }
+  if (cudaGetLastError() != cudaSuccess) return nullptr;
+  p->zmask_key = key;
+  return static_cast<const unsigned long long*>(p->zmask);
+}
+
 template <typename T, int NL> int line_pass_t(nfft_plan* p, int axis, bool fwd) {
   using C = Cx<T>;
   const C* tw = static_cast<const C*>(p->fft_tw[axis]);
@@ -986,9 +1068,11 @@ template <typename T, int NL> int line_pass_t(nfft_plan* p, int axis, bool fwd) 
     const unsigned blocks4 = unsigned(outer_count * L.tiles_x);
     if (p->fft_staged) {  // tile staged by cp.async, in-place four-step
       const size_t smem_s = size_t(NL) * kW4 * sizeof(float2);
-      auto ks = fwd ? fft4_lines_staged_kernel<NL, true> : fft4_lines_staged_kernel<NL, false>;
+      const unsigned long long* zm = axis == 2 ? zmask_for(p) : nullptr;
+      auto ks = zm ? (fwd ? fft4_lines_staged_kernel<NL, true, true> : fft4_lines_staged_kernel<NL, false, true>)
+                   : (fwd ? fft4_lines_staged_kernel<NL, true, false> : fft4_lines_staged_kernel<NL, false, false>);
       if (int rc = set_smem(ks, smem_s)) return rc;
-      ks<<<blocks4, 256, smem_s, p->stream>>>(L, g, tw);
+      ks<<<blocks4, 256, smem_s, p->stream>>>(L, g, tw, zm);
       NFFT_LAUNCH_CHECK();
       return NFFT_OK;
     }

@@ -162,6 +162,9 @@ struct nfft_plan {
   cudaStream_t zero_stream = nullptr;
   cudaEvent_t ev_grid2_used = nullptr, ev_grid2_zeroed = nullptr;
   bool skip_memset = false;
+  bool fft_prune = true;           // z-line mask of the forward / inverse z passes (3-D FP32 staged path)
+  void* zmask = nullptr;           // tiles_x x Nt1 64-bit masks
+  int64_t zmask_key = -1;
   bool spread_zero_copy = true;    // table spreader: clear the tile by a bulk copy of zero_tile
   void* zero_tile = nullptr;       // 128 KB of zeros
   bool fft_staged = true;          // FP32 line FFTs: tile staged by cp.async, in-place four-step

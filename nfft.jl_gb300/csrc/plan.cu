@@ -562,6 +562,7 @@ int nfft_plan_create(nfft_plan** out, int precision, int D, const int64_t* N, in
   if (const char* e = getenv("NFFT_GB300_CENTER")) p->center = e[0] != '0';
   // the adjoint's pre-zeroed second grid (on by default)
   if (const char* e = getenv("NFFT_GB300_PREZERO")) p->prezero = e[0] != '0';
+  if (const char* e = getenv("NFFT_GB300_FFT_PRUNE")) p->fft_prune = e[0] != '0';
   if (const char* e = getenv("NFFT_GB300_SPREAD_ZERO_COPY")) p->spread_zero_copy = e[0] != '0';
   if (const char* e = getenv("NFFT_GB300_FFT_STAGED")) p->fft_staged = e[0] != '0';
   if (const char* e = getenv("NFFT_GB300_SPREAD_REC")) p->spread_rec = e[0] != '0';
@@ -658,6 +659,7 @@ int nfft_plan_destroy(nfft_plan* p) {
   release_node_buffers(p);
   if (p->zero_stream) cudaStreamSynchronize(p->zero_stream);
   cudaFree(p->grid2);
+  cudaFree(p->zmask);
   cudaFree(p->zero_tile);
   if (p->zero_stream) cudaStreamDestroy(p->zero_stream);
   if (p->ev_grid2_used) cudaEventDestroy(p->ev_grid2_used);
