@@ -651,13 +651,14 @@ __global__ void zmask_kernel(const int32_t* __restrict__ tstart, int nt0, int nt
 // access, so no access has a bank conflict.  W x NL x 8 bytes of shared
 // memory (64 KB at NL = 512).
 //
-// zmask (z lines only, or null): bit b of zmask[y * tiles_x + x tile] says
-// whether grid positions z in [8 b, 8 b + 8) of those lines lie in the
-// padded tile of some bin with nodes.  The forward writes only those
-// positions (the gather reads nothing else; a line block with no such
-// position is skipped), the inverse reads only those (the spreading wrote
-// nothing else into the zeroed grid).
-template <int NL, bool FWD, bool MASKED>
+// MASK = 2 (z lines): bit b of zmask[y * tiles_x + x tile] says whether grid
+// positions z in [8 b, 8 b + 8) of those lines lie in the padded tile of some
+// bin with nodes.  The forward writes only those positions (the gather reads
+// nothing else; a line block with no such position is skipped), the inverse
+// reads only those (the spreading wrote nothing else into the zeroed grid)
+// and skips blocks with none: their lines are zero, and so is their
+// transform, which the zeroed grid already holds.  MASK = 0: no mask.
+template <int NL, bool FWD, int MASK>
 __global__ void __launch_bounds__(256, 3) fft4_lines_staged_kernel(LineGeom L, float2* __restrict__ g,
                                                                    const float2* __restrict__ tw,
                                                                    const unsigned long long* __restrict__ zmask) {
@@ -671,21 +672,9 @@ __global__ void __launch_bounds__(256, 3) fft4_lines_staged_kernel(LineGeom L, f
   const int go = L.outer_N > 0 ? wrap_once(o - L.outer_N / 2, L.outer_Nt) : o;
   C* base = g + int64_t(go) * L.outer_stride + int64_t(tile) * W;
   const int head = L.n_img - L.n_img / 2, tail0 = NL - L.n_img / 2;
-  const unsigned long long live = MASKED ? __ldg(zmask + int64_t(o) * L.tiles_x + tile) : ~0ull;
-  if (MASKED && live == 0) {
-    // forward: no position of these lines is read; inverse: the lines are
-    // zero, and so are their transforms at the image positions
-    if (!FWD) {
-      const int nimg = head + (NL - tail0);
-      for (int c = threadIdx.x; c < nimg * 8; c += 256) {
-        const int r = c >> 3, part = c & 7;
-        const int pos = r < head ? r : tail0 + (r - head);
-        *reinterpret_cast<float4*>(base + int64_t(pos) * L.stride + 2 * part) = make_float4(0.f, 0.f, 0.f, 0.f);
-      }
-    }
-    return;
-  }
-  auto used = [&](int pos) { return !MASKED || ((live >> (pos >> 3)) & 1ull) != 0; };
+  const unsigned long long live = MASK == 2 ? __ldg(zmask + int64_t(o) * L.tiles_x + tile) : ~0ull;
+  if (MASK == 2 && live == 0) return;  // nothing of these lines is read (forward) or non-zero (inverse)
+  auto used = [&](int pos) { return MASK != 2 || ((live >> (pos >> 3)) & 1ull) != 0; };
   // stage the tile: NL rows of W complex values (8 chunks of 16 bytes)
   for (int c = threadIdx.x; c < NL * 8; c += 256) {
     const int row = c >> 3, part = c & 7;
@@ -1026,7 +1015,9 @@ LineGeom make_line_geom(const nfft_plan* p, int axis, int W, int64_t* outer_coun
 // The plan's z-line mask (see fft4_lines_staged_kernel), rebuilt when the
 // nodes, the tile shape or the grid shift changed; null when it does not
 // apply (not a 3-D FP32 binned plan on the staged path, z longer than 512,
-// NFFT_GB300_FFT_PRUNE=0, or a transform outside the centred scope).
+// NFFT_GB300_FFT_PRUNE=0) or would have to be built inside a stream capture.
+// Either pass may run with or without it: the passes agree on every value
+// the gather reads and on every value of the inverse.
 static const unsigned long long* zmask_for(nfft_plan* p) {
   if (!p->fft_prune || p->D != 3 || p->precision != 32 || !p->prm.blocking || !p->tile_start || !p->has_nodes)
     return nullptr;
@@ -1036,6 +1027,9 @@ static const unsigned long long* zmask_for(nfft_plan* p) {
   const int64_t key = (((p->nodes_version * 1024 + p->bs[0]) * 1024 + p->bs[1]) * 1024 + p->bs[2]) * 8 +
                       (sh[0] != 0) * 4 + (sh[1] != 0) * 2 + (sh[2] != 0);
   if (p->zmask && p->zmask_key == key) return static_cast<const unsigned long long*>(p->zmask);
+  // (no allocation or rebuild inside a stream capture: unmasked passes then)
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(p->stream, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone) return nullptr;
   const int tiles_x = int(p->Nt[0] / kW4);
   const size_t bytes = sizeof(unsigned long long) * size_t(tiles_x) * size_t(p->Nt[1]);
   if (!p->zmask && cudaMalloc(&p->zmask, bytes) != cudaSuccess) {
@@ -1069,8 +1063,9 @@ template <typename T, int NL> int line_pass_t(nfft_plan* p, int axis, bool fwd) 
     if (p->fft_staged) {  // tile staged by cp.async, in-place four-step
       const size_t smem_s = size_t(NL) * kW4 * sizeof(float2);
       const unsigned long long* zm = axis == 2 ? zmask_for(p) : nullptr;
-      auto ks = zm ? (fwd ? fft4_lines_staged_kernel<NL, true, true> : fft4_lines_staged_kernel<NL, false, true>)
-                   : (fwd ? fft4_lines_staged_kernel<NL, true, false> : fft4_lines_staged_kernel<NL, false, false>);
+      // (the y passes take no mask: the row bitmap costs more than it saves)
+      auto ks = zm && axis == 2 ? (fwd ? fft4_lines_staged_kernel<NL, true, 2> : fft4_lines_staged_kernel<NL, false, 2>)
+                                : (fwd ? fft4_lines_staged_kernel<NL, true, 0> : fft4_lines_staged_kernel<NL, false, 0>);
       if (int rc = set_smem(ks, smem_s)) return rc;
       ks<<<blocks4, 256, smem_s, p->stream>>>(L, g, tw, zm);
       NFFT_LAUNCH_CHECK();
